@@ -1,0 +1,321 @@
+"""Throughput benchmark of the per-ray imaging path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision fp64|mixed] [--workload render256|stress1024]
+
+One "step" is one full render of the workload's image through the fused
+persistent kernel: every ray of the image traced, sampled and solved.
+Default workload (``render256``): FP64 render of the seeded 256^3-cell
+synthetic snapshot at 256x256 pixels (a=0.94, 17 deg, 230 GHz, <= 8192
+steps).  Printed on rank 0 as one JSON line.
+
+``--impl reference`` times the reference algorithm on the host cores
+instead: the C restatement of Mahakala's make_image (oracle/, FP64, all
+host threads) on a bounded, strided subset of the same image's rays.
+The reference itself (Python + JAX) cannot run on the GPU machine.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic FLOPs (add/sub/mul/div/sqrt = 1, FMA = 2, transcendental = 1),
+# counted from the FP64 device code: one accepted RK4 step (4 closed-form
+# accelerations of 184 + RK4 combine 136 + radius_cal 18 + step rule 3) and
+# one in-snapshot sample at one frequency (lookup 34, trilinear 168, metric
+# 20, fluid frame 92, electrons/units 24, synchrotron 36, transfer 5)
+FLOP_PER_STEP = 4 * 184 + 136 + 18 + 3
+FLOP_PER_SAMPLE = 34 + 168 + 20 + 92 + 24 + 36 + 5
+FLOP_PER_EXTRA_NU = 41
+
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--workload", default="render256", choices=["render256", "stress1024"])
+    p.add_argument("--cpu-sample-rays", type=int, default=0, help="rays per CPU baseline sample (0 = auto)")
+    return p.parse_args()
+
+
+def workload(name):
+    from mahakala_gb300 import configs
+    spec = configs.RENDER_256 if name == "render256" else configs.STRESS_1024
+    desc = (f"{'fp64' if True else ''} render {spec.resolution}x{spec.resolution} of a "
+            f"{spec.snapshot.nblocks * spec.snapshot.cells_per_block}^3-cell synthetic snapshot "
+            f"({spec.snapshot.nblocks}^3 meshblocks of {spec.snapshot.cells_per_block}^3), a={spec.bhspin}, "
+            f"i={spec.inclination} deg, fov +-{spec.half_fov} M, "
+            f"{'/'.join(f'{f / 1e9:g}' for f in spec.freqs)} GHz, <= {spec.max_nsteps} steps")
+    return spec, desc
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def clocks_sampler():
+    path = tempfile.mktemp(prefix="mk_clocks_", suffix=".csv")
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        f = open(path, "w")
+        proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                stdout=f, stderr=subprocess.DEVNULL)
+        return proc, f, path
+    except (OSError, FileNotFoundError):
+        return None, None, path
+
+
+def clocks_summary(proc, f, path, gpu_index):
+    if proc is None:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    proc.terminate()
+    try:
+        proc.wait(timeout=5)
+    except subprocess.TimeoutExpired:
+        proc.kill()
+    f.close()
+    sm, smax, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in open(path):
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 9 or parts[0] != str(gpu_index):
+            continue
+        try:
+            sm.append(float(parts[1]))
+            smax = float(parts[2])
+        except ValueError:
+            continue
+        for name, v in zip(names, parts[5:9]):
+            if v.lower() == "active":
+                reasons.add(name)
+    os.unlink(path)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def measure_fma_peak(torch, precision):
+    """FMA probe: achieved FLOP/s of 8 independent FMA chains per thread."""
+    from mahakala_gb300 import _lib
+    lib = _lib.load()
+    sms = lib.mk_device_sm_count()
+    blocks, threads = sms * 8, 256
+    iters = 4096 if precision == _lib.MK_FP64 else 65536
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        _lib.call("mk_probe_fma", precision, blocks, threads, iters, out.data_ptr(), s.cuda_stream)
+        e1.record(s)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        best = max(best, 2.0 * 8 * iters * blocks * threads / t)
+    return best
+
+
+def cpu_sample_pixels(res, want):
+    stride = max(1, int(round((res * res / max(want, 1)) ** 0.5)))
+    ix, iy = np.meshgrid(np.arange(0, res, stride), np.arange(0, res, stride), indexing="ij")
+    return (ix * res + iy).reshape(-1), stride
+
+
+def cpu_baseline(spec, arrays, rays_wanted, threads):
+    """The oracle (C restatement of the reference, FP64) on a strided pixel
+    subset of the same image; returns (rays/s, sample description)."""
+    import oracle
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    snap = oracle.OracleSnapshot(arrays)
+    pix, stride = cpu_sample_pixels(spec.resolution, rays_wanted)
+    s0 = oracle.initialize_geodesics_at_camera(spec.bhspin, spec.inclination, spec.camera_distance,
+                                               -spec.half_fov, spec.half_fov, spec.resolution)[pix]
+    t0 = time.perf_counter()
+    oracle.render_rays(snap, s0, spec.mass_scale, spec.M_bh, spec.r_high, list(spec.freqs), spec.max_nsteps,
+                       spec.r_low)
+    dt = time.perf_counter() - t0
+    return len(pix) / dt, (f"{len(pix)} rays (every {stride}th pixel in x and y) of the same image, "
+                           f"full FP64 physics, {threads} OpenMP threads; {dt:.1f} s")
+
+
+def run_reference(args):
+    """Reference arm: the reference algorithm (C restatement) on host cores."""
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    spec, desc = workload(args.workload)
+    arrays = spec.snapshot.build()
+    threads = os.cpu_count() or 1
+    want = args.cpu_sample_rays or (1024 if args.workload == "render256" else 512)
+    import oracle
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    snap = oracle.OracleSnapshot(arrays)
+    pix, stride = cpu_sample_pixels(spec.resolution, want)
+    s0_all = oracle.initialize_geodesics_at_camera(spec.bhspin, spec.inclination, spec.camera_distance,
+                                                   -spec.half_fov, spec.half_fov, spec.resolution)
+    times = []
+    for k in range(args.warmup + args.steps):
+        # each step a different strided subset (offset by k), so no ray repeats
+        sub = (pix + k) % (spec.resolution * spec.resolution)
+        t0 = time.perf_counter()
+        oracle.render_rays(snap, s0_all[sub], spec.mass_scale, spec.M_bh, spec.r_high, list(spec.freqs),
+                           spec.max_nsteps, spec.r_low)
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    rays = len(pix)
+    value = rays * len(times) / sum(times)
+    sample = (f"{rays} rays per step (every {stride}th pixel, shifted each step) of the same image, "
+              f"full FP64 physics, {threads} OpenMP threads")
+    line = {"metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded snapshot)",
+            "config": {"workload": desc, "precision": "fp64"}, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "rays/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "images_per_s": value / (spec.resolution ** 2) * len(spec.freqs),
+            "note": "the reference is Python+JAX; jax is not installable offline, so its algorithm runs as the "
+                    "C restatement in oracle/ (pinned to the reference's own outputs)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from mahakala_gb300 import _lib, build
+    build.build()
+    _lib.load()
+    from mahakala_gb300.grmhd.athenak import AthenakFluidModel
+    from mahakala_gb300.images import PreparedRender, image_flux_jy, make_image
+
+    spec, desc = workload(args.workload)
+    t_gen = time.perf_counter()
+    arrays = spec.snapshot.build()
+    t_gen = time.perf_counter() - t_gen
+    model = AthenakFluidModel(arrays, spec.snapshot.bhspin, fluid_gamma=spec.snapshot.fluid_gamma)
+    req = spec.request(model)
+    prep = PreparedRender([req], precision=args.precision, with_steps=True)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    peak64 = measure_fma_peak(torch, _lib.MK_FP64)
+    peak32 = measure_fma_peak(torch, _lib.MK_MIXED)
+
+    for _ in range(max(args.warmup, 3)):
+        prep.launch(stream)
+    torch.cuda.synchronize()
+    steps_total, samples_total = prep.work_totals()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    proc, fh, cpath = clocks_sampler() if rank == 0 else (None, None, None)
+    barrier()
+    ev = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)                      # L2 flush between steps (not timed)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        prep.launch(stream)
+        e1.record(stream)
+        ev.append((e0, e1))
+    barrier()
+    clocks = clocks_summary(proc, fh, cpath, local) if rank == 0 else None
+    times = [a.elapsed_time(b) * 1e-3 for a, b in ev]
+    t_step = statistics.mean(times)
+    if world > 1:
+        t = torch.tensor([t_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    rays = spec.resolution ** 2
+    value = world * rays / t_step
+    nnu = len(spec.freqs)
+
+    # end to end through the public API: host request in, NumPy image out
+    e2e_times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        img_np = make_image(model, camera_inclination=spec.inclination, camera_distance=spec.camera_distance,
+                            mass_scale=spec.mass_scale, M_bh=spec.M_bh, r_high=spec.r_high,
+                            observing_frequency=list(spec.freqs) if nnu > 1 else spec.freqs[0], fov=spec.fov,
+                            resolution=spec.resolution, max_nsteps=spec.max_nsteps, precision=args.precision)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_t = statistics.mean(e2e_times)
+    flux = image_flux_jy(prep.images[0], spec.fov, spec.distance_cm, model.get_units(spec.M_bh, spec.mass_scale)["L_unit"])
+
+    flops = steps_total * FLOP_PER_STEP + samples_total * (FLOP_PER_SAMPLE + FLOP_PER_EXTRA_NU * (nnu - 1))
+    achieved = flops / t_step
+    peak = peak64 if args.precision == "fp64" else peak32
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    threads = os.cpu_count() or 1
+    cpu_val, cpu_sample = cpu_baseline(spec, arrays, args.cpu_sample_rays or 512, threads)
+    line = {
+        "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded snapshot, no external data)",
+        "config": {"workload": desc, "precision": args.precision,
+                   "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write, untimed)",
+                   "parallelism": f"replicas x{world} (rays independent; no collective)",
+                   "mass_scale": spec.mass_scale},
+        "images_per_s": world * nnu / t_step,
+        "ray_steps_per_s": world * steps_total / t_step,
+        "work": {"accepted_steps": steps_total, "samples": samples_total, "rays": rays,
+                 "steps_per_ray": steps_total / rays},
+        "flux_jy": [float(x) for x in np.atleast_1d(flux)],
+        "roofline": {"bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": achieved / 1e12,
+                     "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "kernel": "render_fp64_kernel",
+                     "flop_per_launch": flops,
+                     "peak_source": "FMA probe measured in this run (mk_probe_fma); the measured-peak file "
+                                    "holds no FP64/FP32 ALU figure",
+                     "peak_fp32_tflops": peak32 / 1e12, "peak_fp64_tflops": peak64 / 1e12},
+        "cpu_baseline": {"value": cpu_val, "unit": "rays/s", "cores": threads, "kind": "port",
+                         "sample": cpu_sample},
+        "e2e": {"value": world * rays / e2e_t, "unit": "rays/s", "h2d_bytes_per_step": len(prep.table_bytes),
+                "d2h_bytes_per_step": int(img_np.nbytes),
+                "api": "mahakala_gb300.images.make_image (host request -> NumPy image)"},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "snapshot_build_s": t_gen,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

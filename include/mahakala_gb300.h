@@ -1,0 +1,248 @@
+/*
+ * mahakala_gb300.h -- C ABI of the GB300 (sm_103a) per-ray imaging path.
+ *
+ * Every entry point takes plain pointers and sizes.  Pointers named *_dev
+ * are CUDA device pointers owned by the caller; host structs are read
+ * during the call only.  `stream` is a cudaStream_t passed as void* (NULL =
+ * the legacy default stream).  Work is enqueued on that stream and the call
+ * returns without synchronising; results are valid once the stream reaches
+ * that point.  Every function returns MK_OK (0) or an mk_status code, and
+ * mk_last_error() returns a message for the calling thread's last failure.
+ * No function allocates device memory except where its comment says so;
+ * scratch space is passed in by the caller (see mk_render_workspace_bytes).
+ *
+ * The reference is Mahakala (Python + JAX).  Each entry point names the
+ * reference function it replaces (file:line within that project).
+ */
+#ifndef MAHAKALA_GB300_H
+#define MAHAKALA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MK_ABI_VERSION 1
+#define MK_MAX_NU 4
+
+typedef enum {
+    MK_OK = 0,
+    MK_ERR_ARG = 1,          /* invalid argument (null pointer, bad size)   */
+    MK_ERR_CUDA = 2,         /* a CUDA runtime call or launch failed        */
+    MK_ERR_LIMIT = 3,        /* a size exceeds a documented maximum         */
+    MK_ERR_UNSUPPORTED = 4   /* valid request this build does not implement */
+} mk_status;
+
+/* per-ray stop reasons (status arrays) */
+typedef enum {
+    MK_RAY_ACTIVE = 0,
+    MK_RAY_CAPTURED = 1,     /* reference rule: r - r_EH < tol; fixed rule: r < capture*r_h */
+    MK_RAY_ESCAPED = 2,      /* reference rule: r - r_EH > 1500; fixed rule: outbound r > r_escape */
+    MK_RAY_MAXSTEPS = 3,
+    MK_RAY_NAN = 4
+} mk_ray_status;
+
+typedef enum { MK_FP64 = 0, MK_MIXED = 1 } mk_precision;
+
+typedef enum {
+    /* dt = -(r - r_EH)/div, stop (and reject the step) when the next dt
+       would be NaN, |dt|*div < tol or |dt|*div > 1500
+       (geodesic_integrator, geodesics.py:246-269) */
+    MK_POLICY_REFERENCE = 0,
+    /* h = -clamp(hfrac*r, hmin, hmax); captured at r < capture*r_h;
+       escaped at r > r_escape once r increases (no reference counterpart) */
+    MK_POLICY_FIXED = 1
+} mk_policy_kind;
+
+typedef enum { MK_CAMERA_GRID = 0, MK_CAMERA_EQUATOR = 1 } mk_camera_kind;
+
+typedef struct {
+    int32_t kind;            /* mk_policy_kind */
+    int32_t nmax;            /* N, the maximum number of steps */
+    double div, tol;         /* MK_POLICY_REFERENCE */
+    double hfrac, hmin, hmax, capture, r_escape; /* MK_POLICY_FIXED */
+} mk_step_policy;
+
+/* camera of initialize_geodesics_at_camera (geodesics.py:29-55, 137-216).
+   cos_inc/sin_inc: cos and sin of inclination*pi/180, as the host's libm
+   evaluates them (geodesics.py:205). */
+typedef struct {
+    int32_t kind;            /* mk_camera_kind */
+    int32_t pixels;          /* pixels per side (grid) or along the line (equator) */
+    double bhspin, cos_inc, sin_inc, distance, fov_lower, fov_upper;
+} mk_camera;
+
+/* Device view of one resident snapshot (meshblocks with one ghost layer,
+   AoS float32 [mb][k][j][i][prim], prim order dens, velx, vely, velz, eint,
+   bcc1, bcc2, bcc3).  Filled by mk_snapshot_build; plain data, copyable. */
+typedef struct {
+    const float *blocks;     /* (nmb, n+2, n+2, n+2, 8) */
+    const double *geom;      /* (nmb, 6): x1v[0], x2v[0], x3v[0], dx1, dx2, dx3 per block */
+    const double *faces;     /* block faces: nb[0]+1, then nb[1]+1, then nb[2]+1 values */
+    const int32_t *table;    /* (nb[2], nb[1], nb[0]) block id at each logical location */
+    int32_t nmb, n;
+    int32_t nb[3], pad0;
+    double lo[3], width[3];  /* first face and mean block width per axis (lookup guess) */
+} mk_snapshot_view;
+
+/* One render request: the arguments of make_image (images.py:30-35) after
+   the host-side scalar prologue (units, grmhd/grmhd.py:40-55). */
+typedef struct {
+    mk_camera camera;
+    mk_step_policy policy;
+    double fluid_gamma, r_low, r_high;
+    double electron_gamma_m1, ion_gamma_m1;  /* electron_gamma - 1., ion_gamma - 1. */
+    double Ne_unit, B_unit, L_unit;
+    double cos_fallback_pitch;               /* cos(fallback pitch angle) */
+    double sigma_cut;                        /* images.py:116 */
+    int32_t nnu, snapshot;                   /* frequencies; index into the snapshot array */
+    double nu[MK_MAX_NU];                    /* observing frequencies (Hz) */
+    double *image;                           /* (nnu, npx) device output, specific intensity */
+    int32_t *nsteps;                         /* (npx) device output or NULL */
+    int32_t *status;                         /* (npx) device output or NULL */
+    int64_t ray_offset;                      /* first global ray of this request */
+} mk_request;
+
+/* ---------------------------------------------------------------- misc */
+const char *mk_version(void);
+int32_t mk_abi_version(void);
+const char *mk_last_error(void);
+/* number of SMs of the current device (for callers sizing their own grids) */
+int32_t mk_device_sm_count(void);
+/* sizeof of a public struct by name ("mk_request", ...), 0 if unknown; lets
+   a binding check its struct layout against the library's */
+size_t mk_sizeof(const char *name);
+
+/* ------------------------------------------------------------- camera */
+/* initialize_geodesics_at_camera (geodesics.py:29-55) incl. get_initial_grid
+   (:137-216) and initial_condition/_Nullify (:58-85, 219-230).
+   s0_dev: (npx, 8) with npx = pixels^2 (grid) or pixels (equator); pixel
+   index ix*pixels + iy as meshgrid(indexing='ij') orders it. */
+int mk_camera_init(const mk_camera *camera, double *s0_dev, void *stream);
+
+/* get_camera_pixel (geodesics.py:107-134) + initial_condition: image-plane
+   points (x_dev[i], y_dev[i]) -> s0_dev (n, 8). */
+int mk_camera_points(const double *x_dev, const double *y_dev, int64_t n, double bhspin,
+                     double cos_inc, double sin_inc, double distance, double *s0_dev,
+                     void *stream);
+
+/* ---------------------------------------------------------- geodesics */
+/* geodesic_integrator (geodesics.py:233-281) with RK4_gen (:317-336) and
+   the closed-form Kerr-Schild Christoffel contraction in place of
+   rhs/jacfwd/inv (:294-347).
+   MK_POLICY_REFERENCE: rows_dev (nmax, npx, 8) and dt_dev (nmax, npx), if
+   not NULL, receive the reference's trajectory rows (row i = state before
+   step i; rows after a ray stops repeat its frozen state with dt 0).
+   K_dev (npx) gets the first stopped step (nmax if none), why_dev the
+   mk_ray_status reason, state_dev (npx, 8) the state after K steps.
+   MK_POLICY_FIXED: rows/dt must be NULL; K_dev gets the steps taken and
+   state_dev the final state. */
+int mk_integrate(const double *s0_dev, int64_t npx, double bhspin, const mk_step_policy *policy,
+                 double *rows_dev, double *dt_dev, int32_t *K_dev, int32_t *why_dev,
+                 double *state_dev, void *stream);
+
+/* radius_cal (geodesics.py:284-291) on npts points of stride `stride` doubles */
+int mk_radius_cal(const double *x_dev, int64_t npts, int64_t stride, double bhspin,
+                  double *r_dev, void *stream);
+
+/* One bisection pass of find_shadow_bisection_angles (geodesics.py:405-435):
+   integrates the polar-camera rays at radii mid_dev (n) with the reference
+   rule (div 40, tol 1e-2, max_steps) and writes per ray what
+   select_photons_integrator (:354-378) needs: K (first stopped step),
+   best (argmax of dt over the accepted steps, -1 if none), best_dt, and
+   radius_cal at rows K-1, best-1 and at the last row. */
+int mk_shadow_pass(const double *cos_dev, const double *sin_dev, const double *mid_dev, int64_t n,
+                   double bhspin, double cos_inc, double sin_inc, double distance, int32_t max_steps,
+                   int32_t *K_dev, int32_t *best_dev, double *best_dt_dev, double *r_km1_dev,
+                   double *r_best_dev, double *r_last_dev, void *stream);
+
+/* --------------------------------------------------------- snapshots */
+/* Bytes of device storage mk_snapshot_build needs for nmb blocks of n^3. */
+size_t mk_snapshot_bytes(int32_t nmb, int32_t n);
+
+/* Builds the ghost-filled AoS meshblocks on the device from AthenaK arrays
+   (load_athenak_meshblocks, grmhd/athenak.py:67-158; same-level ghost copy
+   :217-233, zero ghosts at the domain edge).  uov_dev (5, nmb, n, n, n) and
+   B_dev (3, nmb, n, n, n) float32; geom_dev (nmb, 6), faces_dev and
+   table_dev as in mk_snapshot_view (kept by reference, not copied);
+   locs_dev (nmb, 3) logical locations.  Single-level meshes only. */
+int mk_snapshot_build(const float *uov_dev, const float *B_dev, const int32_t *locs_dev,
+                      const double *geom_dev, const double *faces_dev, const int32_t *table_dev,
+                      int32_t nmb, int32_t n, const int32_t nb[3], const double lo[3],
+                      const double width[3], void *storage_dev, size_t storage_bytes,
+                      mk_snapshot_view *view_out, void *stream);
+
+/* ------------------------------------------------------ stage kernels */
+/* get_fluid_scalars_from_geodesics (grmhd/athenak.py:639-812): for npts
+   points S_dev (npts, 8) -> out_dev (npts, 5) = dens, u, pitch_angle,
+   kdotu, b.  cos_fallback = cos(fallback_pitch_angle). */
+int mk_fluid_scalars(const mk_snapshot_view *view, double bhspin, const double *S_dev,
+                     int64_t npts, double cos_fallback, double *out_dev, void *stream);
+
+/* get_prims_from_geodesics (grmhd/athenak.py:527-637): out_dev (npts, 8) in
+   the order dens, velx, vely, velz, eint, bcc1..3; block_dev (npts) the
+   meshblock of each point (-1 outside) or NULL. */
+int mk_fluid_prims(const mk_snapshot_view *view, const double *S_dev, int64_t npts,
+                   double *out_dev, int32_t *block_dev, void *stream);
+
+/* rlow_rhigh_model (electrons.py:32-50) */
+int mk_rlow_rhigh(const double *dens_dev, const double *u_dev, const double *beta_dev, int64_t n,
+                  double r_low, double r_high, double electron_gamma_m1, double ion_gamma_m1,
+                  double *theta_dev, void *stream);
+
+/* synchrotron_coefficients (transfer.py:30-86) */
+int mk_synchrotron(const double *Ne_dev, const double *theta_dev, const double *B_dev,
+                   const double *pitch_dev, const double *nu_dev, int64_t n, int32_t invariant,
+                   double rescale_nu, double *em_dev, double *ab_dev, void *stream);
+
+/* solve_specific_intensity (transfer.py:89-119) on (nsteps, npx) arrays;
+   dIs_dev (nsteps-1, npx) or NULL (row r is step nsteps-1-r) */
+int mk_solve_intensity(const double *em_dev, const double *ab_dev, const double *dt_dev,
+                       int64_t nsteps, int64_t npx, double L_unit, double *I_dev, double *dIs_dev,
+                       void *stream);
+
+/* solve_attenuated_emissivity (transfer.py:122-144); out_dev (nsteps-1, npx) */
+int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const double *dt_dev,
+                             int64_t nsteps, int64_t npx, double L_unit, double *out_dev,
+                             void *stream);
+
+/* ------------------------------------------------------- fused render */
+/* Scratch bytes mk_render needs in workspace_dev; the caller allocates it
+   (8-byte aligned) and may reuse it for calls that do not overlap on the
+   device.  After a launch the workspace holds, as uint64 at these word
+   offsets, the launch's totals: MK_WS_STEPS accepted RK4 steps,
+   MK_WS_SAMPLES in-snapshot samples, and at MK_WS_MAX_TAU the bits of a
+   double, the largest per-step optical depth w*alpha of the transfer
+   solve (the reference's explicit Euler update is stable below 1). */
+#define MK_WS_STEPS 1
+#define MK_WS_SAMPLES 2
+#define MK_WS_MAX_TAU 3
+size_t mk_render_workspace_bytes(void);
+
+/* make_image (images.py:30-144) for nreq requests in ONE persistent launch:
+   camera -> geodesics -> sampling -> electrons -> synchrotron -> sigma cut ->
+   transfer, fused per ray; no trajectory is stored.  reqs_dev (nreq)
+   device array with ray_offset the exclusive prefix sum of the requests'
+   pixel counts; total_rays the sum.  snaps_dev (nsnap) device array of
+   views.  precision: mk_precision.  Request images receive the specific
+   intensity the reference's solve_specific_intensity returns. */
+int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
+              const mk_snapshot_view *snaps_dev, int32_t nsnap, int32_t precision,
+              void *workspace_dev, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------ probes */
+/* FMA throughput probe (no reference counterpart): blocks x threads
+   threads each run iters x 8 dependent-chain FMAs in FP64
+   (precision MK_FP64) or FP32 (MK_MIXED); time it with events to get the
+   ALU peak a roofline is reported against.  out_dev: blocks*threads
+   elements of that type. */
+int mk_probe_fma(int32_t precision, int32_t blocks, int32_t threads, int64_t iters, void *out_dev,
+                 void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAHAKALA_GB300_H */

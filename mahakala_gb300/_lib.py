@@ -1,0 +1,124 @@
+"""ctypes binding of ``libmahakala_gb300.so`` (include/mahakala_gb300.h).
+
+The library is the product: every compute call goes through it.  There is
+no CPU fallback; a missing library or a missing GPU raises immediately.
+"""
+
+import ctypes
+import os
+
+from . import build as _build
+
+_c = ctypes
+_VP = _c.c_void_p
+_I32 = _c.c_int32
+_I64 = _c.c_int64
+_D = _c.c_double
+_SZ = _c.c_size_t
+
+MK_OK, MK_ERR_ARG, MK_ERR_CUDA, MK_ERR_LIMIT, MK_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
+MK_RAY_ACTIVE, MK_RAY_CAPTURED, MK_RAY_ESCAPED, MK_RAY_MAXSTEPS, MK_RAY_NAN = 0, 1, 2, 3, 4
+MK_FP64, MK_MIXED = 0, 1
+MK_POLICY_REFERENCE, MK_POLICY_FIXED = 0, 1
+MK_CAMERA_GRID, MK_CAMERA_EQUATOR = 0, 1
+MK_MAX_NU = 4
+MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU = 1, 2, 3
+
+
+class MKError(RuntimeError):
+    """A C-ABI call returned a non-zero mk_status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"[mk_status {code}] {msg}")
+        self.code = code
+
+
+class StepPolicy(_c.Structure):
+    _fields_ = [("kind", _I32), ("nmax", _I32), ("div", _D), ("tol", _D), ("hfrac", _D), ("hmin", _D),
+                ("hmax", _D), ("capture", _D), ("r_escape", _D)]
+
+
+class Camera(_c.Structure):
+    _fields_ = [("kind", _I32), ("pixels", _I32), ("bhspin", _D), ("cos_inc", _D), ("sin_inc", _D),
+                ("distance", _D), ("fov_lower", _D), ("fov_upper", _D)]
+
+
+class SnapshotView(_c.Structure):
+    _fields_ = [("blocks", _VP), ("geom", _VP), ("faces", _VP), ("table", _VP), ("nmb", _I32), ("n", _I32),
+                ("nb", _I32 * 3), ("pad0", _I32), ("lo", _D * 3), ("width", _D * 3)]
+
+
+class Request(_c.Structure):
+    _fields_ = [("camera", Camera), ("policy", StepPolicy), ("fluid_gamma", _D), ("r_low", _D), ("r_high", _D),
+                ("electron_gamma_m1", _D), ("ion_gamma_m1", _D), ("Ne_unit", _D), ("B_unit", _D),
+                ("L_unit", _D), ("cos_fallback_pitch", _D), ("sigma_cut", _D), ("nnu", _I32),
+                ("snapshot", _I32), ("nu", _D * MK_MAX_NU), ("image", _VP), ("nsteps", _VP), ("status", _VP),
+                ("ray_offset", _I64)]
+
+
+# name -> (restype, argtypes); the declarations of include/mahakala_gb300.h
+SIGNATURES = {
+    "mk_version": (_c.c_char_p, []),
+    "mk_abi_version": (_I32, []),
+    "mk_last_error": (_c.c_char_p, []),
+    "mk_device_sm_count": (_I32, []),
+    "mk_camera_init": (_c.c_int, [_c.POINTER(Camera), _VP, _VP]),
+    "mk_camera_points": (_c.c_int, [_VP, _VP, _I64, _D, _D, _D, _D, _VP, _VP]),
+    "mk_integrate": (_c.c_int, [_VP, _I64, _D, _c.POINTER(StepPolicy), _VP, _VP, _VP, _VP, _VP, _VP]),
+    "mk_radius_cal": (_c.c_int, [_VP, _I64, _I64, _D, _VP, _VP]),
+    "mk_shadow_pass": (_c.c_int, [_VP, _VP, _VP, _I64, _D, _D, _D, _D, _I32, _VP, _VP, _VP, _VP, _VP, _VP,
+                                  _VP]),
+    "mk_snapshot_bytes": (_SZ, [_I32, _I32]),
+    "mk_snapshot_build": (_c.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _I32 * 3, _D * 3, _D * 3, _VP,
+                                     _SZ, _c.POINTER(SnapshotView), _VP]),
+    "mk_fluid_scalars": (_c.c_int, [_c.POINTER(SnapshotView), _D, _VP, _I64, _D, _VP, _VP]),
+    "mk_fluid_prims": (_c.c_int, [_c.POINTER(SnapshotView), _VP, _I64, _VP, _VP, _VP]),
+    "mk_rlow_rhigh": (_c.c_int, [_VP, _VP, _VP, _I64, _D, _D, _D, _D, _VP, _VP]),
+    "mk_synchrotron": (_c.c_int, [_VP, _VP, _VP, _VP, _VP, _I64, _I32, _D, _VP, _VP, _VP]),
+    "mk_solve_intensity": (_c.c_int, [_VP, _VP, _VP, _I64, _I64, _D, _VP, _VP, _VP]),
+    "mk_attenuated_emissivity": (_c.c_int, [_VP, _VP, _VP, _I64, _I64, _D, _VP, _VP]),
+    "mk_render_workspace_bytes": (_SZ, []),
+    "mk_render": (_c.c_int, [_VP, _I32, _I64, _VP, _I32, _I32, _VP, _SZ, _VP]),
+    "mk_sizeof": (_SZ, [_c.c_char_p]),
+    "mk_probe_fma": (_c.c_int, [_I32, _I32, _I32, _I64, _VP, _VP]),
+}
+
+_LIB = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load():
+    """Load the library (no GPU needed to load it) and declare signatures."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"mahakala_gb300: the CUDA library {path} is not built; run "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (there is no CPU fallback)")
+    lib = _c.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    for name, cls in (("mk_step_policy", StepPolicy), ("mk_camera", Camera),
+                      ("mk_snapshot_view", SnapshotView), ("mk_request", Request)):
+        n = lib.mk_sizeof(name.encode())
+        if n != _c.sizeof(cls):
+            raise RuntimeError(f"ABI mismatch: sizeof({name}) C={n} ctypes={_c.sizeof(cls)}")
+    _LIB = lib
+    return lib
+
+
+def check(code):
+    if code != MK_OK:
+        raise MKError(code, load().mk_last_error().decode(errors="replace"))
+    return code
+
+
+def call(name, *args):
+    return check(getattr(load(), name)(*args))

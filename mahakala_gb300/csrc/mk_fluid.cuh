@@ -1,0 +1,203 @@
+// mk_fluid.cuh -- GRMHD snapshot sampling, fluid frame, electron
+// temperature and thermal synchrotron coefficients (device functions).
+//
+// Snapshot layout in HBM: meshblocks with one ghost layer, AoS float32,
+// [mb][k][j][i][prim] with prim = dens, velx, vely, velz, eint, bcc1..3.
+// One cell is 32 bytes (one DRAM sector); the two x-neighbours a trilinear
+// corner pair needs are 64 contiguous bytes.
+#pragma once
+
+#include "mk_kerr.cuh"
+
+namespace mk {
+
+// ------------------------------------------------------------- lookup
+// block index b along one axis with faces[b] < x <= faces[b+1], -1 outside
+// (the per-axis form of athenak.py:663-670 on a single-level mesh)
+__device__ __forceinline__ int axis_block(const double *__restrict__ faces, int nb, double lo,
+                                          double width, double x) {
+    if (!(x > __ldg(faces) && x <= __ldg(faces + nb))) return -1;
+    int b = (int)floor((x - lo) / width);
+    b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
+    for (int it = 0; it < nb && x <= __ldg(faces + b); ++it) --b;
+    for (int it = 0; it < nb && x > __ldg(faces + b + 1); ++it) ++b;
+    return b;
+}
+
+__device__ __forceinline__ int find_block(const mk_snapshot_view &s, double x, double y, double z) {
+    const int bi = axis_block(s.faces, s.nb[0], s.lo[0], s.width[0], x);
+    if (bi < 0) return -1;
+    const int bj = axis_block(s.faces + s.nb[0] + 1, s.nb[1], s.lo[1], s.width[1], y);
+    if (bj < 0) return -1;
+    const int bk = axis_block(s.faces + s.nb[0] + s.nb[1] + 2, s.nb[2], s.lo[2], s.width[2], z);
+    if (bk < 0) return -1;
+    return __ldg(s.table + ((int64_t)bk * s.nb[1] + bj) * s.nb[0] + bi);
+}
+
+// float floor_divide / remainder with NumPy (= jnp) semantics
+__device__ __forceinline__ double py_floordiv(double x, double y) {
+    const double mod = fmod(x, y);
+    double div = (x - mod) / y;
+    if (mod != 0.0 && ((y < 0.0) != (mod < 0.0))) div -= 1.0;
+    if (div != 0.0) {
+        double fl = floor(div);
+        if (div - fl > 0.5) fl += 1.0;
+        return fl;
+    }
+    return copysign(0.0, x / y);
+}
+__device__ __forceinline__ double py_mod1(double x) {
+    double m = fmod(x, 1.0);
+    if (m != 0.0 && m < 0.0) m += 1.0;
+    return m;
+}
+
+// ghost-shifted cell index and offset (athenak.py:718-733)
+struct CellPos {
+    int mb;
+    int idx[3];
+    double del[3];
+};
+
+__device__ __forceinline__ bool locate(const mk_snapshot_view &s, double x, double y, double z, CellPos &c) {
+    const int mb = find_block(s, x, y, z);
+    if (mb < 0) return false;
+    c.mb = mb;
+    const double *g = s.geom + 6 * (int64_t)mb;
+    const double xs[3] = {x, y, z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double d = __ldg(g + 3 + a);
+        const double t = xs[a] - __ldg(g + a) + d;
+        c.del[a] = py_mod1(t / d);
+        int i = (int)py_floordiv(t, d);
+        // the face test above guarantees 0 <= i <= n; clamp keeps loads in bounds
+        c.idx[a] = i < 0 ? 0 : (i > s.n ? s.n : i);
+    }
+    return true;
+}
+
+__device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+
+// trilinear interpolation of the 8 primitives (athenak.py:737-752), FP64
+__device__ __forceinline__ void trilinear8(const mk_snapshot_view &s, const CellPos &c, double prim[8]) {
+    const int n2 = s.n + 2;
+    const int64_t sj = (int64_t)n2 * 8, sk = (int64_t)n2 * n2 * 8;
+    const float *base = s.blocks + ((((int64_t)c.mb * n2 + c.idx[2]) * n2 + c.idx[1]) * n2 + c.idx[0]) * 8;
+    float v[2][2][2][8];
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                const float *p = base + dk * sk + dj * sj + di * 8;
+                const float4 lo = ldg4(p), hi = ldg4(p + 4);
+                v[dk][dj][di][0] = lo.x; v[dk][dj][di][1] = lo.y; v[dk][dj][di][2] = lo.z; v[dk][dj][di][3] = lo.w;
+                v[dk][dj][di][4] = hi.x; v[dk][dj][di][5] = hi.y; v[dk][dj][di][6] = hi.z; v[dk][dj][di][7] = hi.w;
+            }
+    const double d1 = c.del[0], d2 = c.del[1], d3 = c.del[2];
+#pragma unroll
+    for (int p = 0; p < 8; p++) {
+        const double aaa = v[0][0][0][p], aab = v[0][0][1][p], aba = v[0][1][0][p], abb = v[0][1][1][p];
+        const double baa = v[1][0][0][p], bab = v[1][0][1][p], bba = v[1][1][0][p], bbb = v[1][1][1][p];
+        const double daa = aaa + (aab - aaa) * d1;
+        const double dab = aba + (abb - aba) * d1;
+        const double dba = baa + (bab - baa) * d1;
+        const double dbb = bba + (bbb - bba) * d1;
+        const double da = daa + (dab - daa) * d2;
+        const double db = dba + (dbb - dba) * d2;
+        prim[p] = da + (db - da) * d3;
+    }
+}
+
+// fluid scalars at one point (athenak.py:759-794); k = photon wavevector
+struct FluidScalars {
+    double dens, u, pitch, kdotu, b;
+};
+
+__device__ __forceinline__ FluidScalars fluid_frame(const double prim[8], double x, double y, double z,
+                                                    const double k[4], double a, double cos_fallback) {
+    const KerrPoint<double> m = kerr_point(x, y, z, a);
+    const double f = m.f, l1 = m.l1, l2 = m.l2, l3 = m.l3;
+    // g^{00} = -1 - f, g^{0i} = f l_i
+    const double alpha = sqrt(1.0 / (1.0 + f));
+    const double U1 = prim[1], U2 = prim[2], U3 = prim[3];
+    const double lU = l1 * U1 + l2 * U2 + l3 * U3;
+    const double gamma = sqrt(1.0 + ((U1 * U1 + U2 * U2 + U3 * U3) + f * lU * lU));
+    const double ga_f = gamma * alpha * f;
+    const double uc0 = gamma / alpha;
+    const double uc1 = U1 - ga_f * l1, uc2 = U2 - ga_f * l2, uc3 = U3 - ga_f * l3;
+    const double lu = uc0 + l1 * uc1 + l2 * uc2 + l3 * uc3;
+    const double flu = f * lu;
+    const double ud0 = -uc0 + flu, ud1 = uc1 + l1 * flu, ud2 = uc2 + l2 * flu, ud3 = uc3 + l3 * flu;
+    const double B1 = prim[5], B2 = prim[6], B3 = prim[7];
+    const double bc0 = B1 * ud1 + B2 * ud2 + B3 * ud3;
+    const double iuc0 = 1.0 / uc0;
+    const double bc1 = (B1 + uc1 * bc0) * iuc0, bc2 = (B2 + uc2 * bc0) * iuc0, bc3 = (B3 + uc3 * bc0) * iuc0;
+    const double lb = bc0 + l1 * bc1 + l2 * bc2 + l3 * bc3;
+    const double flb = f * lb;
+    const double bd0 = -bc0 + flb, bd1 = bc1 + l1 * flb, bd2 = bc2 + l2 * flb, bd3 = bc3 + l3 * flb;
+    FluidScalars o;
+    o.kdotu = k[0] * ud0 + k[1] * ud1 + k[2] * ud2 + k[3] * ud3;
+    const double kdotb = k[0] * bd0 + k[1] * bd1 + k[2] * bd2 + k[3] * bd3;
+    const double bdotb = bc0 * bd0 + bc1 * bd1 + bc2 * bd2 + bc3 * bd3;
+    double pitch = kdotb / (fabs(o.kdotu) * sqrt(bdotb));
+    if (isnan(pitch)) pitch = cos_fallback;
+    if (fabs(pitch) > 1.0) pitch = pitch / fabs(pitch);
+    o.pitch = acos(pitch);
+    o.dens = prim[0];
+    o.u = prim[4];
+    o.b = sqrt(bdotb);
+    return o;
+}
+
+// rlow_rhigh_model (electrons.py:32-50)
+__device__ __forceinline__ double rlow_rhigh(double dens, double u, double beta, double r_low,
+                                             double r_high, double gem1, double gim1) {
+    const double b2 = beta * beta;
+    const double T_ratio = (r_high * b2 + r_low) / (1.0 + b2);
+    double t = CL2 * (((MP * u) * gem1) * gim1);
+    t /= dens * (gim1 + gem1 * T_ratio);
+    return t / ME_CL_CL;
+}
+
+// synchrotron_coefficients (transfer.py:30-86), FP64.  Frequency-independent
+// parts are split out so a multi-frequency pass evaluates them once.
+struct SynchroPre {
+    double nus, th, Ne, th2;
+};
+
+__device__ __forceinline__ SynchroPre synchro_pre(double Ne, double Th, double B, double pitch) {
+    SynchroPre p;
+    const double nuc = EE * B / TWO_PI_ME_CL;
+    p.th2 = Th * Th;
+    p.nus = ((TWO_NINTHS * nuc) * p.th2) * sin(pitch);
+    p.th = Th;
+    p.Ne = Ne;
+    return p;
+}
+
+__device__ __forceinline__ void synchro_eval(const SynchroPre &p, double nu, bool invariant, double rescale_nu,
+                                             double &em_out, double &ab_out) {
+    const double X = nu / p.nus;
+    const double var = exp(-pow(X, THIRD));
+    const double term = sqrt(X) + C2_11_12 * pow(X, SIXTH);
+    double em = p.Ne * p.nus * (term * term) / (2.0 * p.th2);
+    em = em * var * SQRT2 * PI * EE2 / THREE_CL;
+    if (X > 1.e12) em = 0.0;
+    if (p.th < 0.3) em = 0.0;
+    const double bx = HPL * nu / (ME_CL_CL * p.th);
+    const double Bden = (bx < 2.e-3) ? bx / 24. * (24. + bx * (12. + bx * (4. + bx))) : (exp(bx) - 1.0);
+    const double Bnu = (TWO_HPL * pow(nu, 3.) / Bden) / CL2;
+    double ab = em / Bnu;
+    if (invariant) {
+        const double rn = nu * rescale_nu;
+        em = em / (rn * rn);
+        ab = ab * rn;
+    }
+    em_out = isnan(em) ? 0.0 : em;
+    ab_out = isnan(ab) ? 0.0 : ab;
+}
+
+}  // namespace mk

@@ -1,0 +1,290 @@
+// mk_kerr.cuh -- Kerr spacetime in Cartesian Kerr-Schild coordinates,
+// closed-form geodesic acceleration and the RK4 step, for FP64 and FP32.
+//
+// The reference builds g_{mu nu} = eta + f l l (geodesics.py:88-104),
+// differentiates it with jax.jacfwd and inverts it with an LU solve
+// (geodesics.py:294-347).  Here the same metric is differentiated by hand:
+//
+//   rr = r^2 = kk + q,  kk = (x^2+y^2+z^2-a^2)/2,  q = sqrt(kk^2 + a^2 z^2)
+//   d_c r = (rr x_c + a^2 z delta_c3) / (2 r q)
+//   f = 2 r^3 / (r^4 + a^2 z^2),  d_c f = f (3 d_c r / r - (4 r^3 d_c r + 2 a^2 z delta_c3)/den)
+//   l = (1, (r x + a y)/(rr+a^2), (r y - a x)/(rr+a^2), z/r)
+//   g^{mu nu} = eta - f l^mu l^nu  with l^mu = (-1, l1, l2, l3)
+//
+// and with D = k^c d_c (spatial directional derivative), lv = l.k,
+//   F_nu = -[Df l_nu lv + f (Dl_nu lv + l_nu Dl.k)] + 1/2 d_nu f lv^2 + f lv (d_nu l.k)
+//   accel^mu = g^{mu nu} F_nu,
+// which equals -Gamma^mu_ab k^a k^b, the quantity rhs() returns.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "mahakala_gb300.h"
+
+namespace mk {
+
+// cgs constants as the reference spells them (constants.py:22-31,
+// electrons.py:23-29), and the products the reference evaluates in Python
+// scalar arithmetic, written as the exact doubles Python produces.
+constexpr double EE = 4.8032e-10;
+constexpr double CL = 2.99792458e10;
+constexpr double ME = 9.1094e-28;
+constexpr double MP = 1.6726e-24;
+constexpr double HPL = 6.6261e-27;
+constexpr double C2_11_12 = 0x1.e3437e7101343p+0;      // 2.0**(11./12)
+constexpr double SQRT2 = 0x1.6a09e667f3bcdp+0;         // jnp.sqrt(2)
+constexpr double PI = 0x1.921fb54442d18p+1;            // np.pi
+constexpr double TWO_PI_ME_CL = 0x1.8ba87a55ed610p-53; // 2.*np.pi*ME*CL
+constexpr double EE2 = 0x1.105f00eff1951p-62;          // EE**2
+constexpr double THREE_CL = 0x1.4f0b4f6b80000p+36;     // 3.0*CL
+constexpr double ME_CL_CL = 0x1.b78aed233862dp-21;     // ME*CL*CL
+constexpr double TWO_HPL = 0x1.067ca31b6f6a5p-86;      // 2.*HPL
+constexpr double CL2 = 0x1.85c5de8a0455dp+69;          // CL**2
+constexpr double TWO_NINTHS = 0x1.c71c71c71c71cp-3;    // 2./9.
+constexpr double THIRD = 0x1.5555555555555p-2;         // 1./3
+constexpr double SIXTH = 0x1.5555555555555p-3;         // 1./6 (and 1/6 in RK4)
+
+// Kerr-Schild metric data at a point: g = eta + f l l
+template <typename T>
+struct KerrPoint {
+    T r, f, l1, l2, l3;
+};
+
+template <typename T>
+__device__ __forceinline__ KerrPoint<T> kerr_point(T x, T y, T z, T a) {
+    const T aa = a * a;
+    const T zz = z * z;
+    const T kk = T(0.5) * (x * x + y * y + zz - aa);
+    const T rr = sqrt(kk * kk + aa * zz) + kk;
+    const T r = sqrt(rr);
+    KerrPoint<T> m;
+    m.r = r;
+    m.f = (T(2) * rr * r) / (rr * rr + aa * zz);
+    const T ira = T(1) / (rr + aa);
+    m.l1 = (r * x + a * y) * ira;
+    m.l2 = (r * y - a * x) * ira;
+    m.l3 = z / r;
+    return m;
+}
+
+// Geodesic acceleration dk/dlambda = -Gamma^mu_ab k^a k^b at (x, y, z).
+template <typename T>
+__device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3, T a,
+                                           T &a0, T &a1, T &a2, T &a3) {
+    const T aa = a * a;
+    const T zz = z * z;
+    const T kk = T(0.5) * (x * x + y * y + zz - aa);
+    const T q = sqrt(kk * kk + aa * zz);
+    const T rr = q + kk;
+    const T r = sqrt(rr);
+    const T ir = T(1) / r;
+    const T den = rr * rr + aa * zz;
+    const T rra = rr + aa;
+    // one division for the three reciprocals 1/(2 r q), 1/den, 1/(rr + a^2)
+    const T twoRq = T(2) * r * q;
+    const T inv_all = T(1) / (twoRq * den * rra);
+    const T i2rq = den * rra * inv_all;
+    const T iden = twoRq * rra * inv_all;
+    const T ira = twoRq * den * inv_all;
+
+    const T rx = rr * x * i2rq;
+    const T ry = rr * y * i2rq;
+    const T rz = rra * z * i2rq;
+
+    const T f = T(2) * rr * r * iden;
+    const T c1 = T(3) * ir - T(4) * rr * r * iden;
+    const T fx = f * (c1 * rx);
+    const T fy = f * (c1 * ry);
+    const T fz = f * (c1 * rz - T(2) * aa * z * iden);
+
+    const T l1 = (r * x + a * y) * ira;
+    const T l2 = (r * y - a * x) * ira;
+    const T l3 = z * ir;
+    const T tr = T(2) * r;
+    const T g1 = (x - tr * l1) * ira;
+    const T g2 = (y - tr * l2) * ira;
+    const T rira = r * ira, aira = a * ira;
+    const T l1x = g1 * rx + rira, l1y = g1 * ry + aira, l1z = g1 * rz;
+    const T l2x = g2 * rx - aira, l2y = g2 * ry + rira, l2z = g2 * rz;
+    const T h = z * ir * ir;
+    const T l3x = -h * rx, l3y = -h * ry, l3z = ir - h * rz;
+
+    const T lv = k0 + l1 * k1 + l2 * k2 + l3 * k3;
+    const T Df = k1 * fx + k2 * fy + k3 * fz;
+    const T Dl1 = k1 * l1x + k2 * l1y + k3 * l1z;
+    const T Dl2 = k1 * l2x + k2 * l2y + k3 * l2z;
+    const T Dl3 = k1 * l3x + k2 * l3y + k3 * l3z;
+    const T Dlv = Dl1 * k1 + Dl2 * k2 + Dl3 * k3;
+    const T dlx = l1x * k1 + l2x * k2 + l3x * k3;
+    const T dly = l1y * k1 + l2y * k2 + l3y * k3;
+    const T dlz = l1z * k1 + l2z * k2 + l3z * k3;
+
+    const T Dflv = Df * lv;
+    const T fDlv = f * Dlv;
+    const T half_lv2 = T(0.5) * lv * lv;
+    const T flv = f * lv;
+    const T F0 = -(Dflv + fDlv);
+    const T F1 = -(Dflv * l1 + f * (Dl1 * lv) + l1 * fDlv) + fx * half_lv2 + flv * dlx;
+    const T F2 = -(Dflv * l2 + f * (Dl2 * lv) + l2 * fDlv) + fy * half_lv2 + flv * dly;
+    const T F3 = -(Dflv * l3 + f * (Dl3 * lv) + l3 * fDlv) + fz * half_lv2 + flv * dlz;
+    const T lF = -F0 + l1 * F1 + l2 * F2 + l3 * F3;
+    const T flF = f * lF;
+    a0 = -F0 + flF;
+    a1 = F1 - l1 * flF;
+    a2 = F2 - l2 * flF;
+    a3 = F3 - l3 * flF;
+}
+
+// RK4_gen (geodesics.py:317-336) for one ray: out = s + 1/6 (k1+2k2+2k3+k4)
+template <typename T>
+__device__ __forceinline__ void rk4_step(const T s[8], T dt, T a, T out[8]) {
+    T acc[8], tmp[8], d0, d1, d2, d3;
+    kerr_accel(s[1], s[2], s[3], s[4], s[5], s[6], s[7], a, d0, d1, d2, d3);
+    {
+        const T k[8] = {dt * s[4], dt * s[5], dt * s[6], dt * s[7], dt * d0, dt * d1, dt * d2, dt * d3};
+#pragma unroll
+        for (int i = 0; i < 8; i++) { acc[i] = k[i]; tmp[i] = s[i] + T(0.5) * k[i]; }
+    }
+    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, d1, d2, d3);
+    {
+        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * d1, dt * d2, dt * d3};
+#pragma unroll
+        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2) * k[i]; tmp[i] = s[i] + T(0.5) * k[i]; }
+    }
+    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, d1, d2, d3);
+    {
+        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * d1, dt * d2, dt * d3};
+#pragma unroll
+        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2) * k[i]; tmp[i] = s[i] + k[i]; }
+    }
+    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, d1, d2, d3);
+    {
+        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * d1, dt * d2, dt * d3};
+#pragma unroll
+        for (int i = 0; i < 8; i++) out[i] = s[i] + T(SIXTH) * (acc[i] + k[i]);
+    }
+}
+
+// radius_cal (geodesics.py:284-291): the KS radius the step rule uses
+template <typename T>
+__device__ __forceinline__ T radius_cal(T x, T y, T z, T a) {
+    const T R = sqrt(x * x + y * y + z * z);
+    const T q = R * R - a * a;
+    return sqrt((q + sqrt(q * q + T(4) * (a * a) * (z * z))) / T(2));
+}
+
+__host__ __device__ __forceinline__ double radius_eh(double a) { return 1.0 + sqrt(1.0 - a * a); }
+
+// dt rule of geodesic_step (geodesics.py:249-252); why = stop reason
+template <typename T>
+__device__ __forceinline__ T reference_dt(T r, T r_eh, T div, T tol, int &why) {
+    const T dt = -(r - r_eh) / div;
+    why = MK_RAY_ACTIVE;
+    if (isnan(dt)) { why = MK_RAY_NAN; return T(0); }
+    const T adiv = fabs(dt) * div;
+    if (adiv < tol) { why = MK_RAY_CAPTURED; return T(0); }
+    if (adiv > T(1500)) { why = MK_RAY_ESCAPED; return T(0); }
+    return dt;
+}
+
+// ------------------------------------------------------------- camera
+// _Image_to_BH (geodesics.py:204-209)
+__device__ __forceinline__ void image_to_bh(double x, double y, double z, double ci, double si,
+                                            double d, double o[3]) {
+    o[0] = __dadd_rn(__dadd_rn(__dmul_rn(-y, ci), __dmul_rn(z, si)), __dmul_rn(d, si));
+    o[1] = x;
+    o[2] = __dadd_rn(__dadd_rn(__dmul_rn(y, si), __dmul_rn(z, ci)), __dmul_rn(d, ci));
+}
+
+// _Nullify with p=1 (geodesics.py:58-85): rescales v[1..3] so g(v,v) = 0
+__device__ __forceinline__ void nullify(const double x[4], double a, double v[4]) {
+    const KerrPoint<double> m = kerr_point(x[1], x[2], x[3], a);
+    const double l[4] = {1.0, m.l1, m.l2, m.l3};
+    double g[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            g[i][j] = __dadd_rn((i == j) ? (i == 0 ? -1.0 : 1.0) : 0.0, __dmul_rn(m.f, __dmul_rn(l[i], l[j])));
+    const double A = __dmul_rn(__dmul_rn(v[0], g[0][0]), v[0]);
+    const double b = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[1], g[1][0]), __dmul_rn(v[2], g[2][0])),
+                                         __dmul_rn(v[3], g[3][0])), v[0]);
+    double w[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+        w[j] = __dadd_rn(__dadd_rn(__dmul_rn(v[1], g[1][1 + j]), __dmul_rn(v[2], g[2][1 + j])),
+                         __dmul_rn(v[3], g[3][1 + j]));
+    const double C = __dadd_rn(__dadd_rn(__dmul_rn(w[0], v[1]), __dmul_rn(w[1], v[2])), __dmul_rn(w[2], v[3]));
+    const double bb = __dmul_rn(b, b), AC = __dmul_rn(A, C);
+    const bool close = fabs(bb - AC) <= (1e-8 + 1e-5 * fabs(AC));
+    const double dd = close ? 0.0 : bb - AC;
+    const double bs = (b < 0.0) ? 0.0 : 1.0;  // heaviside(b, 1)
+    const double D = -(b + bs * sqrt(dd));
+    const double x1 = D / A, x2 = C / D;
+    double d1, d2;
+    if (isnan(x1) || isnan(x2)) { d1 = d2 = nan(""); }
+    else { d1 = fmin(x1, x2); d2 = fmax(x1, x2); }
+    const double S = (d1 > 0.0) ? d1 : ((d2 > 0.0) ? d2 : nan(""));
+    v[1] = v[1] / S;
+    v[2] = v[2] / S;
+    v[3] = v[3] / S;
+}
+
+// grid pixel centre: np.linspace(lo, hi, 2n+1)[1::2][i] = (2i+1)*step + lo
+__device__ __forceinline__ double grid_coord(int i, int n, double lo, double hi) {
+    const double step = (hi - lo) / (double)(2 * n);
+    return __dadd_rn(__dmul_rn((double)(2 * i + 1), step), lo);
+}
+
+// jnp.linspace(lo, hi, 2n+1)[1::2][i] (equator camera, geodesics.py:185):
+// lo*(1 - t) + hi*t with t = (2i+1)/(2n)
+__device__ __forceinline__ double jnp_grid_coord(int i, int n, double lo, double hi) {
+    const double t = (double)(2 * i + 1) / (double)(2 * n);
+    return __dadd_rn(__dmul_rn(lo, 1.0 - t), __dmul_rn(hi, t));
+}
+
+// one camera pixel at image-plane (x, y) (geodesics.py:168-179, 121-132)
+__device__ __forceinline__ void camera_pixel(double x, double y, double ci, double si, double d,
+                                             double a, double s[8]) {
+    double org[3], ini[3], per[3];
+    image_to_bh(0.0, 0.0, 0.0, ci, si, d, org);
+    image_to_bh(x, y, 0.0, ci, si, d, ini);
+    image_to_bh(__dadd_rn(x, y), __dsub_rn(y, x), 0.0, ci, si, d, per);
+    double v1[3], v2[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) { v1[i] = __dadd_rn(-ini[i], org[i]); v2[i] = __dsub_rn(per[i], ini[i]); }
+    s[0] = 0.0;
+    s[1] = ini[0];
+    s[2] = ini[1];
+    s[3] = ini[2];
+    double v[4];
+    v[0] = 1.0;
+    v[1] = __dsub_rn(__dmul_rn(v1[1], v2[2]), __dmul_rn(v1[2], v2[1]));
+    v[2] = __dsub_rn(__dmul_rn(v1[2], v2[0]), __dmul_rn(v1[0], v2[2]));
+    v[3] = __dsub_rn(__dmul_rn(v1[0], v2[1]), __dmul_rn(v1[1], v2[0]));
+    nullify(s, a, v);
+    s[4] = v[0];
+    s[5] = v[1];
+    s[6] = v[2];
+    s[7] = v[3];
+}
+
+// initial state of pixel p of a camera
+__device__ __forceinline__ void camera_ray(const mk_camera &c, int64_t p, double s[8]) {
+    const int n = c.pixels;
+    if (c.kind == MK_CAMERA_EQUATOR) {
+        double x[4] = {0.0, c.distance, jnp_grid_coord((int)p, n, c.fov_lower, c.fov_upper), 0.0};
+        double v[4] = {1.0, 1.0, 0.0, 0.0};
+        nullify(x, c.bhspin, v);
+        s[0] = x[0]; s[1] = x[1]; s[2] = x[2]; s[3] = x[3];
+        s[4] = v[0]; s[5] = v[1]; s[6] = v[2]; s[7] = v[3];
+        return;
+    }
+    const int ix = (int)(p / n), iy = (int)(p % n);
+    camera_pixel(grid_coord(ix, n, c.fov_lower, c.fov_upper), grid_coord(iy, n, c.fov_lower, c.fov_upper),
+                 c.cos_inc, c.sin_inc, c.distance, c.bhspin, s);
+}
+
+}  // namespace mk

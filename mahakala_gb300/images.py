@@ -1,0 +1,177 @@
+"""Image rendering: ``make_image`` (mahakala/images.py:30-144) and the
+multi-request ``render_requests`` behind it.
+
+The whole per-ray path -- camera, geodesics, GRMHD sampling, electron
+temperature, synchrotron, sigma cut, transfer -- runs in one persistent
+sm_103a kernel (``mk_render``); no trajectory is materialised, so
+``max_chunk_bytes`` (the reference's memory knob) has nothing to bound and
+is accepted for compatibility only.
+"""
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._device import device, ptr, stream_ptr
+from .constants import JY, Msun
+from .geodesics import camera_pixels, make_camera, step_policy
+
+__all__ = ["make_image", "RenderRequest", "PreparedRender", "render_requests", "image_flux_jy"]
+
+PRECISIONS = {"fp64": _lib.MK_FP64, "mixed": _lib.MK_MIXED}
+
+
+@dataclass
+class RenderRequest:
+    """Arguments of make_image for one image (one or more frequencies)."""
+    model: object                      # AthenakFluidModel (resident snapshot)
+    camera_inclination: float = 60
+    camera_distance: float = 1000
+    mass_scale: float = 1.e26
+    M_bh: float = 6.2e9 * Msun
+    r_high: float = 40
+    observing_frequency: object = 230.e9   # scalar or a list of up to 4 frequencies
+    fov: float = 20
+    resolution: int = 160
+    max_nsteps: int = 10000
+    r_low: float = 1
+    bhspin: float = None               # default: the model's spin
+    div: float = 40.
+    tol: float = 1e-4
+    out: dict = field(default_factory=dict)
+
+    @property
+    def freqs(self):
+        return np.atleast_1d(np.asarray(self.observing_frequency, dtype=np.float64))
+
+    @property
+    def npx(self):
+        return int(self.resolution) ** 2
+
+
+def _fill_request(req, rq, snap_index, image, nsteps, status, offset):
+    model = req.model
+    a = model.bhspin if req.bhspin is None else req.bhspin
+    if model.fluid_gamma is None:
+        # images.py:88 needs fluid_gamma (None raises a TypeError there)
+        raise TypeError("fluid_model.fluid_gamma must be set to render an image")
+    freqs = req.freqs
+    if not 1 <= len(freqs) <= _lib.MK_MAX_NU:
+        raise ValueError(f"1..{_lib.MK_MAX_NU} observing frequencies per request")
+    rq.camera = make_camera(a, req.camera_inclination, req.camera_distance, -req.fov / 2., req.fov / 2.,
+                            req.resolution)
+    rq.policy = step_policy(req.max_nsteps, req.div, req.tol)
+    rq.fluid_gamma = float(model.fluid_gamma)
+    rq.r_low, rq.r_high = float(req.r_low), float(req.r_high)
+    rq.electron_gamma_m1, rq.ion_gamma_m1 = 4. / 3 - 1., 5. / 3 - 1.
+    units = model.get_units(req.M_bh, req.mass_scale)
+    rq.Ne_unit, rq.B_unit, rq.L_unit = units["Ne_unit"], units["B_unit"], units["L_unit"]
+    rq.cos_fallback_pitch = float(np.cos(np.pi / 3.))
+    rq.sigma_cut = 100.
+    rq.nnu = len(freqs)
+    rq.snapshot = snap_index
+    for i, f in enumerate(freqs):
+        rq.nu[i] = float(f)
+    rq.image, rq.nsteps, rq.status = ptr(image), ptr(nsteps), ptr(status)
+    rq.ray_offset = int(offset)
+
+
+class PreparedRender:
+    """A batch of requests laid out on the device once: the request table,
+    the snapshot views, the output images and the launch workspace.
+    ``launch()`` enqueues the single persistent render kernel; it can be
+    called repeatedly (each call overwrites the outputs)."""
+
+    def __init__(self, requests, precision="fp64", with_steps=False):
+        if not requests:
+            raise ValueError("no requests")
+        dev = device()
+        self.requests = list(requests)
+        self.precision = PRECISIONS[precision]
+        snaps, snap_index = [], {}
+        for r in requests:
+            key = id(r.model.snapshot)
+            if key not in snap_index:
+                snap_index[key] = len(snaps)
+                snaps.append(r.model.snapshot)
+        table = (_lib.Request * len(requests))()
+        offset = 0
+        self.images = []
+        for i, r in enumerate(requests):
+            img = torch.empty((len(r.freqs), r.resolution, r.resolution), dtype=torch.float64, device=dev)
+            ns = st = None
+            if with_steps:
+                ns = torch.empty((r.resolution, r.resolution), dtype=torch.int32, device=dev)
+                st = torch.empty((r.resolution, r.resolution), dtype=torch.int32, device=dev)
+            _fill_request(r, table[i], snap_index[id(r.model.snapshot)], img, ns, st, offset)
+            r.out["image"] = img
+            if with_steps:
+                r.out["nsteps"], r.out["status"] = ns, st
+            self.images.append(img)
+            offset += r.npx
+        self.total_rays = offset
+        self.table_bytes = bytes(table)
+        self.reqs_dev = torch.frombuffer(bytearray(self.table_bytes), dtype=torch.uint8).to(dev)
+        self.snaps_dev = torch.cat([sn.view_dev for sn in snaps]) if len(snaps) > 1 else snaps[0].view_dev
+        self.nsnap = len(snaps)
+        self.ws = torch.zeros(_lib.load().mk_render_workspace_bytes() // 8, dtype=torch.int64, device=dev)
+
+    def launch(self, stream=None):
+        _lib.call("mk_render", ptr(self.reqs_dev), len(self.requests), self.total_rays, ptr(self.snaps_dev),
+                  self.nsnap, self.precision, ptr(self.ws), self.ws.numel() * 8, stream_ptr(stream))
+        return self.images
+
+    def work_totals(self):
+        """(accepted steps, in-snapshot samples) of the last launch (syncs)."""
+        w = self.ws.cpu()
+        return int(w[_lib.MK_WS_STEPS]), int(w[_lib.MK_WS_SAMPLES])
+
+    def max_step_optical_depth(self):
+        """Largest per-step w*alpha of the last launch (syncs); the explicit
+        Euler transfer of the reference is stable while this stays below 1."""
+        return float(self.ws.cpu()[_lib.MK_WS_MAX_TAU:_lib.MK_WS_MAX_TAU + 1].view(torch.float64)[0])
+
+
+def render_requests(requests, precision="fp64", stream=None, with_steps=False):
+    """Render several requests in ONE persistent launch.
+
+    Each request's ``out`` dict receives ``image`` ((nnu, res, res) float64
+    CUDA tensor) and, with ``with_steps``, ``nsteps`` and ``status``.
+    Returns the list of image tensors.  The launch is asynchronous on
+    ``stream`` (default: the current stream)."""
+    if not requests:
+        return []
+    s = stream if stream is not None else torch.cuda.current_stream()
+    with torch.cuda.stream(s):
+        prep = PreparedRender(requests, precision, with_steps)
+        images = prep.launch(s)
+    # the request table and workspace stay alive until the launch retires
+    for t in (prep.reqs_dev, prep.snaps_dev, prep.ws):
+        t.record_stream(s)
+    return images
+
+
+def make_image(fluid_model, camera_inclination=60, camera_distance=1000, mass_scale=1.e26, M_bh=6.2e9 * Msun,
+               r_high=40, observing_frequency=230.e9, fov=20, resolution=160, max_nsteps=10000,
+               max_chunk_bytes=None, precision="fp64", r_low=1):
+    """images.py:30-144 -> NumPy image (resolution, resolution) indexed [i_x, i_y];
+    with a list of frequencies, (nnu, resolution, resolution)."""
+    req = RenderRequest(fluid_model, camera_inclination, camera_distance, mass_scale, M_bh, r_high,
+                        observing_frequency, fov, resolution, max_nsteps, r_low)
+    img = render_requests([req], precision=precision)[0]
+    out = img.cpu().numpy()
+    if np.ndim(observing_frequency) == 0:
+        out = out[0]
+    return out
+
+
+def image_flux_jy(image, fov, distance_cm, L_unit):
+    """Total flux (Jy) of an image of specific intensity: sum I dOmega with
+    dOmega = (fov/res)^2 L_unit^2 / D^2 per pixel."""
+    img = image.detach().cpu().numpy() if isinstance(image, torch.Tensor) else np.asarray(image)
+    res = img.shape[-1]
+    dpix = fov / res * L_unit / distance_cm
+    return img.sum(axis=(-2, -1)) * dpix * dpix / JY

@@ -1,0 +1,137 @@
+"""GPU stage kernels (C-ABI) against the oracle and the reference's golden
+vectors: camera, integrator, radius, snapshot build, sampling, electrons,
+synchrotron, transfer.  Every call goes through libmahakala_gb300.so."""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def test_camera_matches_reference_and_oracle(cuda, orc):
+    import mahakala_gb300 as mk
+    d = golden("camera")
+    for n in range(5):
+        p = d[f"case{n}_params"]
+        kind = "equator" if bool(d[f"case{n}_equator"]) else "grid"
+        s0 = _np(mk.initialize_geodesics_at_camera(*p[:5], int(p[5]), camera_type=kind))
+        ref = d[f"case{n}_s0"]
+        assert np.array_equal(np.isnan(s0), np.isnan(ref))
+        assert np.nanmax(rel_err(s0, ref)) < 1e-14, n
+        o = orc.initialize_geodesics_at_camera(*p[:5], int(p[5]), camera_type=kind)
+        assert np.nanmax(rel_err(s0, o)) < 1e-14, n
+
+
+def test_camera_rejects_bad_type(cuda):
+    import mahakala_gb300 as mk
+    with pytest.raises(ValueError):
+        mk.initialize_geodesics_at_camera(0.5, 60, 1000, -10, 10, 4, camera_type="fisheye")
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_integrator_rows_match_reference(cuda, case):
+    import mahakala_gb300 as mk
+    d = golden("integrator")
+    a, inc, half, px, N, div, tol = d[f"case{case}_params"]
+    S, dt = mk.geodesic_integrator(int(N), d[f"case{case}_s0"], div, tol, a)
+    S, dt = _np(S), _np(dt)
+    assert S.shape[0] == int(d[f"case{case}_rows"])
+    assert np.array_equal((dt != 0).sum(axis=0), d[f"case{case}_nsteps"])
+    last = d[f"case{case}_last"]
+    assert np.array_equal(np.isnan(S[-1]), np.isnan(last))
+    assert np.nanmax(rel_err(S[-1], last, floor=1e-3)) < 1e-8
+    keep = d[f"case{case}_keep"]
+    assert np.nanmax(rel_err(S[:, keep], d[f"case{case}_S_keep"], floor=1e-3)) < 1e-10
+
+
+def test_integrator_matches_oracle_many_rays(cuda, orc):
+    import mahakala_gb300 as mk
+    from mahakala_gb300.geodesics import step_policy, trace
+    a = 0.94
+    s0 = orc.initialize_geodesics_at_camera(a, 60, 1000, -10, 10, 24)
+    o = orc.integrate(s0, 3000, 40.0, 1e-4, a)
+    g = trace(s0, a, step_policy(3000, 40.0, 1e-4))
+    K, why, state = _np(g["K"]), _np(g["why"]), _np(g["state"])
+    assert np.array_equal(why, o["why"])                  # captured/escaped masks
+    same = K == o["K"]
+    assert same.mean() >= 0.995, f"{(~same).sum()} rays changed step count"
+    assert np.nanmax(rel_err(state[same], o["state"][same], floor=1e-3)) < 1e-9
+
+
+def test_radius_cal(cuda, orc):
+    from mahakala_gb300.geodesics import radius_cal
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=(1000, 8)) * 50
+    r = _np(radius_cal(x, 0.7))
+    assert np.max(rel_err(r, orc.radius_cal(x, 0.7))) < 1e-15
+
+
+def test_snapshot_build_equals_reference_ghost_fill(cuda, tiny_arrays):
+    from mahakala_gb300.grmhd.athenak import DeviceSnapshot
+    snap = DeviceSnapshot(tiny_arrays)
+    blocks = _np(snap.blocks())                        # (nmb, k, j, i, prim)
+    ref = golden("snapshot")["all_meshblocks"]          # (nmb, prim, k, j, i)
+    assert np.array_equal(blocks.transpose(0, 4, 1, 2, 3), ref)
+
+
+def test_fluid_scalars_and_prims_match_reference(cuda, tiny_arrays):
+    from mahakala_gb300.grmhd.athenak import AthenakFluidModel
+    d = golden("scalars")
+    model = AthenakFluidModel(tiny_arrays, 0.9, fluid_gamma=13. / 9)
+    pr = model.get_prims_from_geodesics(d["S"])
+    for k in ("dens", "U1", "U2", "U3", "u", "B1", "B2", "B3"):
+        assert np.array_equal(_np(pr[k]), d["pr_" + k]), k
+    sc = model.get_fluid_scalars_from_geodesics(d["S"])
+    for k in ("dens", "u", "kdotu", "b"):
+        x = _np(sc[k])
+        assert np.array_equal(np.isnan(x), np.isnan(d["sc_" + k])), k
+        assert np.nanmax(rel_err(x, d["sc_" + k])) < 1e-12, k
+    assert np.nanmax(np.abs(_np(sc["pitch_angle"]) - d["sc_pitch_angle"])) < 1e-10
+
+
+def test_electrons_match_reference(cuda):
+    from mahakala_gb300.electrons import rlow_rhigh_model
+    d = golden("electrons")
+    for tag, kw in (("default", {}), ("rhigh10", dict(r_high=10)), ("rhigh80_rlow3", dict(r_high=80, r_low=3)),
+                    ("gammas", dict(electron_gamma=5. / 3, ion_gamma=4. / 3))):
+        t = _np(rlow_rhigh_model(d["dens"], d["u"], d["beta"], **kw))
+        ref = d["theta_" + tag]
+        assert np.array_equal(np.isnan(t), np.isnan(ref))
+        assert np.nanmax(rel_err(t, ref)) < 1e-15
+
+
+def test_synchrotron_matches_reference(cuda):
+    import mahakala_gb300 as mk
+    d = golden("synchrotron")
+    args = [d[k] for k in ("Ne", "Theta", "B", "pitch", "nu")]
+    for tag, kw in (("inv", dict(invariant=True, rescale_nu=1 / 230e9)), ("raw", dict(invariant=False))):
+        em, ab = mk.synchrotron_coefficients(*args, **kw)
+        for x, ref in ((_np(em), d["em_" + tag]), (_np(ab), d["ab_" + tag])):
+            assert np.array_equal(x == 0, ref == 0)
+            assert np.max(rel_err(x, ref)) < 1e-11
+
+
+def test_transfer_matches_reference(cuda):
+    import mahakala_gb300 as mk
+    d = golden("transfer")
+    L = float(d["L_unit"])
+    I = _np(mk.solve_specific_intensity(d["em"], d["ab"], d["dt"], L))
+    assert np.max(rel_err(I, d["I"], floor=1e-300)) < 1e-14
+    I2, dIs = mk.solve_specific_intensity(d["em"], d["ab"], d["dt"], L, dIs=True)
+    assert np.max(np.abs(_np(dIs) - d["dIs"])) <= 1e-14 * np.max(np.abs(d["dIs"]))
+    att = _np(mk.solve_attenuated_emissivity(d["em"], d["ab"], d["dt"], L))
+    assert np.max(rel_err(att, d["att"], floor=1e-300)) < 1e-13
+
+
+def test_errors_are_loud(cuda):
+    """Bad arguments come back as MKError, not as silent garbage."""
+    from mahakala_gb300 import _lib
+    with pytest.raises(_lib.MKError):
+        _lib.call("mk_solve_intensity", None, None, None, 3, 3, 1.0, None, None, None)
