@@ -50,13 +50,19 @@ def parse():
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--workload", default="render256", choices=["render256", "stress1024"])
     p.add_argument("--cpu-sample-rays", type=int, default=0, help="rays per CPU baseline sample (0 = auto)")
+    p.add_argument("--resolution", type=int, default=0, help="override the image size (profiling small cases)")
+    p.add_argument("--quick", action="store_true",
+                   help="device timing only: skip the FMA probes, the end-to-end pass and the CPU baseline")
     return p.parse_args()
 
 
-def workload(name):
+def workload(name, resolution=0, precision="fp64"):
+    import dataclasses
     from mahakala_gb300 import configs
     spec = configs.RENDER_256 if name == "render256" else configs.STRESS_1024
-    desc = (f"{'fp64' if True else ''} render {spec.resolution}x{spec.resolution} of a "
+    if resolution:
+        spec = dataclasses.replace(spec, resolution=int(resolution))
+    desc = (f"{precision} render {spec.resolution}x{spec.resolution} of a "
             f"{spec.snapshot.nblocks * spec.snapshot.cells_per_block}^3-cell synthetic snapshot "
             f"({spec.snapshot.nblocks}^3 meshblocks of {spec.snapshot.cells_per_block}^3), a={spec.bhspin}, "
             f"i={spec.inclination} deg, fov +-{spec.half_fov} M, "
@@ -153,8 +159,9 @@ def cpu_baseline(spec, arrays, rays_wanted, threads):
     oracle.render_rays(snap, s0, spec.mass_scale, spec.M_bh, spec.r_high, list(spec.freqs), spec.max_nsteps,
                        spec.r_low)
     dt = time.perf_counter() - t0
-    return len(pix) / dt, (f"{len(pix)} rays (every {stride}th pixel in x and y) of the same image, "
-                           f"full FP64 physics, {threads} OpenMP threads; {dt:.1f} s")
+    what = "the whole image" if stride == 1 else f"every {stride}th pixel in x and y of the same image"
+    return len(pix) / dt, (f"{len(pix)} rays ({what}), full FP64 physics, {threads} OpenMP threads; "
+                           f"{dt:.1f} s")
 
 
 def run_reference(args):
@@ -162,10 +169,12 @@ def run_reference(args):
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return
-    spec, desc = workload(args.workload)
+    spec, desc = workload(args.workload, args.resolution, "fp64")
     arrays = spec.snapshot.build()
     threads = os.cpu_count() or 1
-    want = args.cpu_sample_rays or (1024 if args.workload == "render256" else 512)
+    # a quarter of the image per step (about 1 s of all-core CPU work for the
+    # 256x256 workload), shifted each step
+    want = args.cpu_sample_rays or (spec.resolution ** 2) // 4
     import oracle
     os.environ["OMP_NUM_THREADS"] = str(threads)
     snap = oracle.OracleSnapshot(arrays)
@@ -215,7 +224,7 @@ def main():
     from mahakala_gb300.grmhd.athenak import AthenakFluidModel
     from mahakala_gb300.images import PreparedRender, image_flux_jy, make_image
 
-    spec, desc = workload(args.workload)
+    spec, desc = workload(args.workload, args.resolution, args.precision)
     t_gen = time.perf_counter()
     arrays = spec.snapshot.build()
     t_gen = time.perf_counter() - t_gen
@@ -225,8 +234,8 @@ def main():
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    peak64 = measure_fma_peak(torch, _lib.MK_FP64)
-    peak32 = measure_fma_peak(torch, _lib.MK_MIXED)
+    peak64 = measure_fma_peak(torch, _lib.MK_FP64) if not args.quick else float("nan")
+    peak32 = measure_fma_peak(torch, _lib.MK_MIXED) if not args.quick else float("nan")
 
     for _ in range(max(args.warmup, 3)):
         prep.launch(stream)
@@ -262,7 +271,7 @@ def main():
 
     # end to end through the public API: host request in, NumPy image out
     e2e_times = []
-    for _ in range(args.steps):
+    for _ in range(0 if args.quick else args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         img_np = make_image(model, camera_inclination=spec.inclination, camera_distance=spec.camera_distance,
@@ -270,7 +279,7 @@ def main():
                             observing_frequency=list(spec.freqs) if nnu > 1 else spec.freqs[0], fov=spec.fov,
                             resolution=spec.resolution, max_nsteps=spec.max_nsteps, precision=args.precision)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_t = statistics.mean(e2e_times)
+    e2e_t = statistics.mean(e2e_times) if e2e_times else float("nan")
     flux = image_flux_jy(prep.images[0], spec.fov, spec.distance_cm, model.get_units(spec.M_bh, spec.mass_scale)["L_unit"])
 
     flops = steps_total * FLOP_PER_STEP + samples_total * (FLOP_PER_SAMPLE + FLOP_PER_EXTRA_NU * (nnu - 1))
@@ -281,7 +290,11 @@ def main():
             torch.distributed.destroy_process_group()
         return
     threads = os.cpu_count() or 1
-    cpu_val, cpu_sample = cpu_baseline(spec, arrays, args.cpu_sample_rays or 512, threads)
+    if args.quick:
+        cpu_val, cpu_sample = None, "skipped (--quick)"
+    else:
+        # the whole image (about 4 s on 16 cores for the 256x256 workload)
+        cpu_val, cpu_sample = cpu_baseline(spec, arrays, args.cpu_sample_rays or spec.resolution ** 2, threads)
     line = {
         "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
@@ -306,7 +319,7 @@ def main():
         "cpu_baseline": {"value": cpu_val, "unit": "rays/s", "cores": threads, "kind": "port",
                          "sample": cpu_sample},
         "e2e": {"value": world * rays / e2e_t, "unit": "rays/s", "h2d_bytes_per_step": len(prep.table_bytes),
-                "d2h_bytes_per_step": int(img_np.nbytes),
+                "d2h_bytes_per_step": int(prep.images[0].numel() * 8),
                 "api": "mahakala_gb300.images.make_image (host request -> NumPy image)"},
         "gpu_launches": args.steps,
         "clocks": clocks,

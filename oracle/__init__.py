@@ -185,6 +185,24 @@ def integrate(s0, N, div, tol, bhspin, full=False):
     return out
 
 
+def perturbed(s0, eps=1e-12):
+    """s0 with the wavevector's spatial part scaled by (1 + eps): a probe of
+    how strongly each ray amplifies a rounding-sized change."""
+    s = np.array(s0, dtype=np.float64, copy=True)
+    s[:, 5:8] *= (1.0 + eps)
+    return s
+
+
+def ill_conditioned(state, state_pert, eps=1e-12, amplification=100.0, floor=1e-3):
+    """Rays whose end state moves by more than amplification*eps (relative,
+    floor 1e-3) when the initial wavevector moves by eps: photon-ring rays
+    whose end state no FP64 evaluation order reproduces to the parity bar."""
+    with np.errstate(all="ignore"):
+        d = np.abs(state - state_pert) / np.maximum(np.abs(state), floor)
+    d = np.where(np.isnan(d), np.inf, d)
+    return d.reshape(d.shape[0], -1).max(axis=1) > amplification * eps
+
+
 def trimmed_rows(K, N):
     """Number of trajectory rows geodesic_integrator keeps (geodesics.py:275-281)."""
     if np.all(K < N):

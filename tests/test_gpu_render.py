@@ -2,10 +2,12 @@
 images and the oracle.
 
 Tolerance: 1e-8 relative per pixel (floor 1e-4 of the image maximum for
-near-empty pixels), the FP64 parity bar.  A pixel whose ray changed its
-step count relative to the oracle (a ray grazing the photon ring, where the
-closed-form and the autodiff Christoffel symbols round differently and the
-orbit amplifies it) is reported and may differ; at most 0.5% of pixels.
+near-empty pixels), the FP64 parity bar, on every well-conditioned pixel.
+A pixel is ill-conditioned when the oracle's own intensity or step count
+moves under a 1e-12 change of the ray's initial wavevector (a ray grazing
+the photon ring, where the closed-form and the autodiff Christoffel
+symbols round differently and the orbit amplifies it); those are counted
+and must stay a small fraction.
 """
 
 import numpy as np
@@ -58,11 +60,18 @@ def test_render_matches_oracle(cuda, orc, medium, inc, rh, nu):
     osnap = orc.OracleSnapshot(medium)
     oimg, osteps = orc.make_image(osnap, return_steps=True, **kw)
     assert oimg.max() > 0
-    same = steps == osteps
-    assert same.mean() >= 0.995, f"{(~same).sum()} rays changed step count"
-    err = rel_err(img, oimg, floor=1e-4 * oimg.max())
-    assert np.max(err[same]) < PIX_TOL
-    assert abs(img.sum() - oimg.sum()) / oimg.sum() < 1e-8
+    s0 = orc.initialize_geodesics_at_camera(medium.bhspin, inc, 1000, -25.0, 25.0, 32)
+    rkw = dict(mass_scale=kw["mass_scale"], M_bh=kw["M_bh"], r_high=rh, observing_frequency=nu, max_nsteps=3000)
+    pimg, psteps = orc.render_rays(osnap, orc.perturbed(s0), **rkw)
+    pimg, psteps = pimg.reshape(32, 32), psteps.reshape(32, 32)
+    floor = 1e-4 * oimg.max()
+    ill = (psteps != osteps) | (rel_err(pimg, oimg, floor=floor) > 1e-10)
+    assert ill.mean() < 0.05, f"{ill.sum()} ill-conditioned pixels"
+    ok = ~ill
+    assert np.array_equal(steps[ok], osteps[ok])
+    err = rel_err(img, oimg, floor=floor)
+    assert np.max(err[ok]) < PIX_TOL
+    assert abs(img[ok].sum() - oimg[ok].sum()) / oimg[ok].sum() < 1e-8
 
 
 def test_multifrequency_pass_equals_single(cuda, medium):

@@ -60,9 +60,14 @@ def test_integrator_matches_oracle_many_rays(cuda, orc):
     g = trace(s0, a, step_policy(3000, 40.0, 1e-4))
     K, why, state = _np(g["K"]), _np(g["why"]), _np(g["state"])
     assert np.array_equal(why, o["why"])                  # captured/escaped masks
-    same = K == o["K"]
-    assert same.mean() >= 0.995, f"{(~same).sum()} rays changed step count"
-    assert np.nanmax(rel_err(state[same], o["state"][same], floor=1e-3)) < 1e-9
+    # photon-ring rays amplify rounding-sized differences; the oracle flags
+    # them by its own response to a 1e-12 change of the initial wavevector
+    op = orc.integrate(orc.perturbed(s0), 3000, 40.0, 1e-4, a)
+    ill = orc.ill_conditioned(o["state"], op["state"]) | (o["K"] != op["K"])
+    assert ill.mean() < 0.05, f"{ill.sum()} ill-conditioned rays"
+    ok = ~ill
+    assert np.array_equal(K[ok], o["K"][ok])
+    assert np.nanmax(rel_err(state[ok], o["state"][ok], floor=1e-3)) < 1e-9
 
 
 def test_radius_cal(cuda, orc):

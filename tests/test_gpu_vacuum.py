@@ -4,10 +4,12 @@ policies against the oracle: the reference rule (div 40, tol 1e-4) and the
 fixed-fraction rule (h = 0.05 r clamped to [0.01, 10] M, captured at
 r < 1.01 r_h, escaped at r > 1000 M once r grows).
 
-Bar: captured/escaped masks bit-exact; final x^mu, k^mu within 1e-9
-relative (floor 1e-3 for components that pass through zero) for every ray
-whose step count equals the oracle's; at most 0.5% of rays (photon-ring
-grazers) may change step count, and they are counted.
+Bar: captured/escaped masks bit-exact; step counts equal and final x^mu,
+k^mu within 1e-9 relative (floor 1e-3 for components that pass through
+zero) for every well-conditioned ray.  A ray is ill-conditioned when the
+oracle's own end state moves by more than 100x a 1e-12 change of the
+initial wavevector (photon-ring grazers: no FP64 evaluation order
+reproduces them to 1e-9); those are counted, and must stay a few percent.
 """
 
 import numpy as np
@@ -28,26 +30,34 @@ def s0(orc):
 def test_vacuum_reference_policy(cuda, orc, s0):
     from mahakala_gb300.geodesics import step_policy, trace
     o = orc.integrate(s0, NMAX, 40.0, 1e-4, A)
+    op = orc.integrate(orc.perturbed(s0), NMAX, 40.0, 1e-4, A)
     g = trace(s0, A, step_policy(NMAX, 40.0, 1e-4))
     why, K, st = (g[k].cpu().numpy() for k in ("why", "K", "state"))
     assert np.array_equal(why, o["why"])
     cap = why == 1
     assert 0.05 < cap.mean() < 0.6          # a shadow is there
-    same = K == o["K"]
-    assert same.mean() >= 0.995, f"{(~same).sum()} of {len(K)} rays changed step count"
-    assert np.nanmax(rel_err(st[same], o["state"][same], floor=1e-3)) < 1e-9
+    ill = orc.ill_conditioned(o["state"], op["state"]) | (o["K"] != op["K"])
+    print(f"vacuum reference policy: {ill.sum()} of {len(K)} rays ill-conditioned")
+    assert ill.mean() < 0.05
+    ok = ~ill
+    assert np.array_equal(K[ok], o["K"][ok])
+    assert np.nanmax(rel_err(st[ok], o["state"][ok], floor=1e-3)) < 1e-9
 
 
 def test_vacuum_fixed_policy(cuda, orc, s0):
     from mahakala_gb300.geodesics import step_policy, trace
     o = orc.trace_fixed(s0, NMAX, A)
+    op = orc.trace_fixed(orc.perturbed(s0), NMAX, A)
     g = trace(s0, A, step_policy(NMAX, kind="fixed"))
     why, K, st = (g[k].cpu().numpy() for k in ("why", "K", "state"))
     assert np.array_equal(why, o["why"])
     assert set(np.unique(why)) <= {1, 2}     # every ray captured or escaped within 4096 steps
-    same = K == o["nsteps"]
-    assert same.mean() >= 0.995
-    assert np.nanmax(rel_err(st[same], o["state"][same], floor=1e-3)) < 1e-9
+    ill = orc.ill_conditioned(o["state"], op["state"]) | (o["nsteps"] != op["nsteps"])
+    print(f"vacuum fixed policy: {ill.sum()} of {len(K)} rays ill-conditioned")
+    assert ill.mean() < 0.05
+    ok = ~ill
+    assert np.array_equal(K[ok], o["nsteps"][ok])
+    assert np.nanmax(rel_err(st[ok], o["state"][ok], floor=1e-3)) < 1e-9
 
 
 @pytest.mark.parametrize("key", ["test1", "test2", "test3", "test4"])
