@@ -4,10 +4,13 @@
                     [--precision fp64|mixed] [--workload render256|stress1024]
 
 One "step" is one full render of the workload's image through the fused
-persistent kernel: every ray of the image traced, sampled and solved.
-Default workload (``render256``): FP64 render of the seeded 256^3-cell
-synthetic snapshot at 256x256 pixels (a=0.94, 17 deg, 230 GHz, <= 8192
-steps).  Printed on rank 0 as one JSON line.
+persistent kernels: every ray of the image traced, sampled and solved.
+Default workload (``render256``): render of the seeded 256^3-cell synthetic
+snapshot at 256x256 pixels (a=0.94, 17 deg, 230 GHz, <= 8192 steps), timed
+in both forms -- plain FP64 and mixed FP32/FP64 -- with the mixed form's
+flux and per-pixel error against the FP64 image of the same run.  The
+headline value is the mixed form's rays/s.  Printed on rank 0 as one JSON
+line.
 
 ``--impl reference`` times the reference algorithm on the host cores
 instead: the C restatement of Mahakala's make_image (oracle/, FP64, all
@@ -47,7 +50,8 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"],
+                   help="both: time FP64 and mixed, headline the mixed form and report its error vs FP64")
     p.add_argument("--workload", default="render256", choices=["render256", "stress1024"])
     p.add_argument("--cpu-sample-rays", type=int, default=0, help="rays per CPU baseline sample (0 = auto)")
     p.add_argument("--resolution", type=int, default=0, help="override the image size (profiling small cases)")
@@ -207,6 +211,25 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def time_render(torch, prep, stream, steps, warmup, flush, barrier):
+    """W warm-up launches, then K launches each timed by CUDA events on the
+    launching stream with an L2 flush (untimed) before each."""
+    for _ in range(max(warmup, 3)):
+        prep.launch(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ev = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        prep.launch(stream)
+        e1.record(stream)
+        ev.append((e0, e1))
+    barrier()
+    return [a.elapsed_time(b) * 1e-3 for a, b in ev]
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -218,56 +241,48 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    from mahakala_gb300 import _lib, build
+    from mahakala_gb300 import _lib, build, metrics
     build.build()
     _lib.load()
     from mahakala_gb300.grmhd.athenak import AthenakFluidModel
     from mahakala_gb300.images import PreparedRender, image_flux_jy, make_image
 
-    spec, desc = workload(args.workload, args.resolution, args.precision)
+    forms = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    head = forms[-1]
+    spec, desc = workload(args.workload, args.resolution, head)
     t_gen = time.perf_counter()
     arrays = spec.snapshot.build()
     t_gen = time.perf_counter() - t_gen
     model = AthenakFluidModel(arrays, spec.snapshot.bhspin, fluid_gamma=spec.snapshot.fluid_gamma)
-    req = spec.request(model)
-    prep = PreparedRender([req], precision=args.precision, with_steps=True)
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-
     peak64 = measure_fma_peak(torch, _lib.MK_FP64) if not args.quick else float("nan")
     peak32 = measure_fma_peak(torch, _lib.MK_MIXED) if not args.quick else float("nan")
-
-    for _ in range(max(args.warmup, 3)):
-        prep.launch(stream)
-    torch.cuda.synchronize()
-    steps_total, samples_total = prep.work_totals()
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    proc, fh, cpath = clocks_sampler() if rank == 0 else (None, None, None)
-    barrier()
-    ev = []
-    for _ in range(args.steps):
-        flush.fill_(1.0)                      # L2 flush between steps (not timed)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        prep.launch(stream)
-        e1.record(stream)
-        ev.append((e0, e1))
-    barrier()
-    clocks = clocks_summary(proc, fh, cpath, local) if rank == 0 else None
-    times = [a.elapsed_time(b) * 1e-3 for a, b in ev]
-    t_step = statistics.mean(times)
-    if world > 1:
-        t = torch.tensor([t_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t.item())
     rays = spec.resolution ** 2
-    value = world * rays / t_step
     nnu = len(spec.freqs)
+    res = {}
+    proc, fh, cpath = clocks_sampler() if rank == 0 else (None, None, None)
+    for form in forms:
+        req = spec.request(model)
+        prep = PreparedRender([req], precision=form, with_steps=True)
+        times = time_render(torch, prep, stream, args.steps, args.warmup, flush, barrier)
+        t_step = statistics.mean(times)
+        if world > 1:
+            t = torch.tensor([t_step], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            t_step = float(t.item())
+        steps_total, samples_total = prep.work_totals()
+        split = prep.precision_split() if form == "mixed" else (0, 0, steps_total)
+        res[form] = dict(prep=prep, req=req, t_step=t_step, steps=steps_total, samples=samples_total,
+                         split=split, image=prep.images[0].clone(), status=req.out["status"].clone(),
+                         max_tau=prep.max_step_optical_depth())
+    clocks = clocks_summary(proc, fh, cpath, local) if rank == 0 else None
 
     # end to end through the public API: host request in, NumPy image out
     e2e_times = []
@@ -277,14 +292,42 @@ def main():
         img_np = make_image(model, camera_inclination=spec.inclination, camera_distance=spec.camera_distance,
                             mass_scale=spec.mass_scale, M_bh=spec.M_bh, r_high=spec.r_high,
                             observing_frequency=list(spec.freqs) if nnu > 1 else spec.freqs[0], fov=spec.fov,
-                            resolution=spec.resolution, max_nsteps=spec.max_nsteps, precision=args.precision)
+                            resolution=spec.resolution, max_nsteps=spec.max_nsteps, precision=head)
         e2e_times.append(time.perf_counter() - t0)
     e2e_t = statistics.mean(e2e_times) if e2e_times else float("nan")
-    flux = image_flux_jy(prep.images[0], spec.fov, spec.distance_cm, model.get_units(spec.M_bh, spec.mass_scale)["L_unit"])
+    L_unit = model.get_units(spec.M_bh, spec.mass_scale)["L_unit"]
 
-    flops = steps_total * FLOP_PER_STEP + samples_total * (FLOP_PER_SAMPLE + FLOP_PER_EXTRA_NU * (nnu - 1))
-    achieved = flops / t_step
-    peak = peak64 if args.precision == "fp64" else peak32
+    def roofline(form):
+        r = res[form]
+        flops = r["steps"] * FLOP_PER_STEP + r["samples"] * (FLOP_PER_SAMPLE + FLOP_PER_EXTRA_NU * (nnu - 1))
+        achieved = flops / r["t_step"]
+        peak = peak64 if form == "fp64" else peak32
+        out = {"bound": "fp64" if form == "fp64" else "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12,
+               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+               "kernel": "render_fp64_kernel" if form == "fp64" else
+               "render_f32_kernel x2 + render_fp64_kernel (queue) (three launches)",
+               "flop_per_launch": flops,
+               "peak_source": "FMA probe measured in this run (mk_probe_fma); the measured-peak file holds no "
+                              "FP64/FP32 ALU figure",
+               "peak_fp32_tflops": peak32 / 1e12, "peak_fp64_tflops": peak64 / 1e12}
+        if form == "fp64":
+            out["traffic_note"] = ("ncu on the 192x192 case: 242 MB DRAM read per launch; the kernel is "
+                                   "FP64-pipe bound (profiles/render_fp64_kernel_render192.md)")
+        return out
+
+    def form_line(form):
+        r = res[form]
+        to64, back32, steps64 = r["split"]
+        return {"rays_per_s": world * rays / r["t_step"], "ms_per_step": 1e3 * r["t_step"],
+                "images_per_s": world * nnu / r["t_step"], "ray_steps_per_s": world * r["steps"] / r["t_step"],
+                "accepted_steps": r["steps"], "samples": r["samples"], "steps_per_ray": r["steps"] / rays,
+                "rays_to_fp64": to64, "rays_back_to_fp32": back32, "steps_in_fp64": steps64,
+                "max_step_optical_depth": r["max_tau"],
+                "flux_jy": [float(x) for x in np.atleast_1d(image_flux_jy(r["image"], spec.fov, spec.distance_cm,
+                                                                         L_unit))],
+                "roofline": roofline(form)}
+
+    t_head = res[head]["t_step"]
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -296,35 +339,39 @@ def main():
         # the whole image (about 4 s on 16 cores for the 256x256 workload)
         cpu_val, cpu_sample = cpu_baseline(spec, arrays, args.cpu_sample_rays or spec.resolution ** 2, threads)
     line = {
-        "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "metric": "rays/s", "value": world * rays / t_head, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_head, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32+f64",
         "data": "synthetic (seeded snapshot, no external data)",
-        "config": {"workload": desc, "precision": args.precision,
+        "config": {"workload": desc, "precision": head,
                    "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write, untimed)",
                    "parallelism": f"replicas x{world} (rays independent; no collective)",
                    "mass_scale": spec.mass_scale},
-        "images_per_s": world * nnu / t_step,
-        "ray_steps_per_s": world * steps_total / t_step,
-        "work": {"accepted_steps": steps_total, "samples": samples_total, "rays": rays,
-                 "steps_per_ray": steps_total / rays},
-        "flux_jy": [float(x) for x in np.atleast_1d(flux)],
-        "roofline": {"bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": achieved / 1e12,
-                     "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                     "kernel": "render_fp64_kernel",
-                     "flop_per_launch": flops,
-                     "peak_source": "FMA probe measured in this run (mk_probe_fma); the measured-peak file "
-                                    "holds no FP64/FP32 ALU figure",
-                     "peak_fp32_tflops": peak32 / 1e12, "peak_fp64_tflops": peak64 / 1e12},
+        "images_per_s": world * nnu / t_head,
+    }
+    for form in forms:
+        line[form] = form_line(form)
+    if "fp64" in res and "mixed" in res:
+        a, b = res["mixed"], res["fp64"]
+        errs = [metrics.compare(a["image"][c], b["image"][c], a["status"], b["status"], spec.fov)
+                for c in range(nnu)]
+        line["mixed_vs_fp64"] = {"speedup": b["t_step"] / a["t_step"],
+                                 "flux_rel_err": max(e["flux_rel_err"] for e in errs),
+                                 "max_pixel_rel_err": max(e["max_pixel_rel_err"] for e in errs),
+                                 "shadow_diameter": errs[0]["shadow_diameter"],
+                                 "shadow_diameter_fp64": errs[0]["shadow_diameter_fp64"],
+                                 "pixel_floor": "max(|I_fp64|, 1e-4 max I_fp64)"}
+    line.update({
+        "roofline": roofline(head),
         "cpu_baseline": {"value": cpu_val, "unit": "rays/s", "cores": threads, "kind": "port",
                          "sample": cpu_sample},
-        "e2e": {"value": world * rays / e2e_t, "unit": "rays/s", "h2d_bytes_per_step": len(prep.table_bytes),
-                "d2h_bytes_per_step": int(prep.images[0].numel() * 8),
-                "api": "mahakala_gb300.images.make_image (host request -> NumPy image)"},
-        "gpu_launches": args.steps,
+        "e2e": {"value": world * rays / e2e_t, "unit": "rays/s", "h2d_bytes_per_step": len(res[head]["prep"].table_bytes),
+                "d2h_bytes_per_step": int(rays * nnu * 8),
+                "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
+        "gpu_launches": args.steps * (1 if head == "fp64" else 3),
         "clocks": clocks,
         "snapshot_build_s": t_gen,
-    }
+    })
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -80,6 +80,7 @@ typedef struct {
 typedef struct {
     const float *blocks;     /* (nmb, n+2, n+2, n+2, 8) */
     const double *geom;      /* (nmb, 6): x1v[0], x2v[0], x3v[0], dx1, dx2, dx3 per block */
+    const float *geom_f32;   /* (nmb, 8): x1v[0], x2v[0], x3v[0], 1/dx1, 1/dx2, 1/dx3, 0, 0 (mixed form) */
     const double *faces;     /* block faces: nb[0]+1, then nb[1]+1, then nb[2]+1 values */
     const int32_t *table;    /* (nb[2], nb[1], nb[0]) block id at each logical location */
     int32_t nmb, n;
@@ -209,19 +210,27 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
                              void *stream);
 
 /* ------------------------------------------------------- fused render */
-/* Scratch bytes mk_render needs in workspace_dev; the caller allocates it
-   (8-byte aligned) and may reuse it for calls that do not overlap on the
-   device.  After a launch the workspace holds, as uint64 at these word
-   offsets, the launch's totals: MK_WS_STEPS accepted RK4 steps,
-   MK_WS_SAMPLES in-snapshot samples, and at MK_WS_MAX_TAU the bits of a
-   double, the largest per-step optical depth w*alpha of the transfer
-   solve (the reference's explicit Euler update is stable below 1). */
+/* Scratch bytes mk_render needs in workspace_dev for total_rays rays at
+   the given precision: a 256-byte header of counters (MK_FP64), plus two
+   ray queues of total_rays records each for the hand-offs between the
+   FP32 and FP64 phases (MK_MIXED).  The caller allocates it (16-byte
+   aligned) and may reuse it for calls that do not overlap on the device.
+   After a launch the header holds, as uint64 at these word offsets, the
+   launch's totals: MK_WS_STEPS accepted RK4 steps, MK_WS_SAMPLES
+   in-snapshot samples, MK_WS_MAX_TAU the bits of a double, the largest
+   per-step optical depth w*alpha of the transfer solve (the reference's
+   explicit Euler update is stable below 1), MK_WS_TO_FP64 rays handed to
+   FP64 and MK_WS_STEPS_FP64 steps taken in FP64 (mixed form). */
 #define MK_WS_STEPS 1
 #define MK_WS_SAMPLES 2
 #define MK_WS_MAX_TAU 3
-size_t mk_render_workspace_bytes(void);
+#define MK_WS_TO_FP64 4
+#define MK_WS_TO_FP32 6
+#define MK_WS_STEPS_FP64 8
+size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision);
 
-/* make_image (images.py:30-144) for nreq requests in ONE persistent launch:
+/* make_image (images.py:30-144) for nreq requests in ONE persistent launch
+   (three launches in the mixed form: FP32, FP64 near the hole, FP32):
    camera -> geodesics -> sampling -> electrons -> synchrotron -> sigma cut ->
    transfer, fused per ray; no trajectory is stored.  reqs_dev (nreq)
    device array with ray_offset the exclusive prefix sum of the requests'

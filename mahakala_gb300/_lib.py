@@ -22,7 +22,7 @@ MK_FP64, MK_MIXED = 0, 1
 MK_POLICY_REFERENCE, MK_POLICY_FIXED = 0, 1
 MK_CAMERA_GRID, MK_CAMERA_EQUATOR = 0, 1
 MK_MAX_NU = 4
-MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU = 1, 2, 3
+MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_TO_FP32, MK_WS_STEPS_FP64 = 1, 2, 3, 4, 6, 8
 
 
 class MKError(RuntimeError):
@@ -44,7 +44,8 @@ class Camera(_c.Structure):
 
 
 class SnapshotView(_c.Structure):
-    _fields_ = [("blocks", _VP), ("geom", _VP), ("faces", _VP), ("table", _VP), ("nmb", _I32), ("n", _I32),
+    _fields_ = [("blocks", _VP), ("geom", _VP), ("geom_f32", _VP), ("faces", _VP), ("table", _VP), ("nmb", _I32),
+                ("n", _I32),
                 ("nb", _I32 * 3), ("pad0", _I32), ("lo", _D * 3), ("width", _D * 3)]
 
 
@@ -77,7 +78,7 @@ SIGNATURES = {
     "mk_synchrotron": (_c.c_int, [_VP, _VP, _VP, _VP, _VP, _I64, _I32, _D, _VP, _VP, _VP]),
     "mk_solve_intensity": (_c.c_int, [_VP, _VP, _VP, _I64, _I64, _D, _VP, _VP, _VP]),
     "mk_attenuated_emissivity": (_c.c_int, [_VP, _VP, _VP, _I64, _I64, _D, _VP, _VP]),
-    "mk_render_workspace_bytes": (_SZ, []),
+    "mk_render_workspace_bytes": (_SZ, [_I64, _I32]),
     "mk_render": (_c.c_int, [_VP, _I32, _I64, _VP, _I32, _I32, _VP, _SZ, _VP]),
     "mk_sizeof": (_SZ, [_c.c_char_p]),
     "mk_probe_fma": (_c.c_int, [_I32, _I32, _I32, _I64, _VP, _VP]),

@@ -97,17 +97,20 @@ __device__ __forceinline__ void trilinear8(const mk_snapshot_view &s, const Cell
                 v[dk][dj][di][4] = hi.x; v[dk][dj][di][5] = hi.y; v[dk][dj][di][6] = hi.z; v[dk][dj][di][7] = hi.w;
             }
     const double d1 = c.del[0], d2 = c.del[1], d3 = c.del[2];
+    // a + (b - a) d rounded twice (no fused multiply-add), as the reference
+    // evaluates it, so the interpolated primitives are bit-identical
+    auto lerp = [](double a, double b, double d) { return __dadd_rn(a, __dmul_rn(__dsub_rn(b, a), d)); };
 #pragma unroll
     for (int p = 0; p < 8; p++) {
         const double aaa = v[0][0][0][p], aab = v[0][0][1][p], aba = v[0][1][0][p], abb = v[0][1][1][p];
         const double baa = v[1][0][0][p], bab = v[1][0][1][p], bba = v[1][1][0][p], bbb = v[1][1][1][p];
-        const double daa = aaa + (aab - aaa) * d1;
-        const double dab = aba + (abb - aba) * d1;
-        const double dba = baa + (bab - baa) * d1;
-        const double dbb = bba + (bbb - bba) * d1;
-        const double da = daa + (dab - daa) * d2;
-        const double db = dba + (dbb - dba) * d2;
-        prim[p] = da + (db - da) * d3;
+        const double daa = lerp(aaa, aab, d1);
+        const double dab = lerp(aba, abb, d1);
+        const double dba = lerp(baa, bab, d1);
+        const double dbb = lerp(bba, bbb, d1);
+        const double da = lerp(daa, dab, d2);
+        const double db = lerp(dba, dbb, d2);
+        prim[p] = lerp(da, db, d3);
     }
 }
 
@@ -198,6 +201,155 @@ __device__ __forceinline__ void synchro_eval(const SynchroPre &p, double nu, boo
     }
     em_out = isnan(em) ? 0.0 : em;
     ab_out = isnan(ab) ? 0.0 : ab;
+}
+
+}  // namespace mk
+
+// ------------------------------------------------------------------------
+// FP32 sampling and emission for the mixed-precision render.  Same
+// mathematics as above, evaluated in float with the cgs prefactors folded
+// into per-frequency constants so no intermediate leaves the float range
+// (2 HPL / c^2 = 1.5e-47 would underflow on its own).
+// ------------------------------------------------------------------------
+namespace mk {
+
+// per-frequency constants of the FP32 synchrotron (computed in FP64 once
+// per ray, see synchro_consts)
+struct SynchroF32 {
+    float k_em;   // sqrt2 pi EE^2/(3 CL) * nu_obs: emissivity prefactor in rescaled units
+    float k_bx;   // HPL nu_obs / (ME CL^2): bx = k_bx nu' / Theta_e
+    float k_bnu;  // 2 HPL nu_obs^3 / CL^2: B_nu = k_bnu nu'^3 / Bden
+    float inv_nu; // 1 / nu_obs (only for nus' = nus / nu_obs)
+};
+
+__device__ __forceinline__ SynchroF32 synchro_consts(double nu_obs) {
+    SynchroF32 c;
+    c.k_em = (float)(SQRT2 * PI * EE2 / THREE_CL * nu_obs);
+    c.k_bx = (float)(HPL * nu_obs / ME_CL_CL);
+    c.k_bnu = (float)(TWO_HPL * nu_obs * nu_obs * nu_obs / CL2);
+    c.inv_nu = (float)(1.0 / nu_obs);
+    return c;
+}
+
+// block lookup + ghost-shifted cell position in float (uniform single-level
+// grid: block = floor((x - lo)/width); cells from the block's first centre)
+struct CellPosF {
+    int mb;
+    int idx[3];
+    float del[3];
+};
+
+struct SnapF32 {
+    float lo[3], inv_w[3];
+};
+
+__device__ __forceinline__ SnapF32 snap_f32(const mk_snapshot_view &s) {
+    SnapF32 f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        f.lo[a] = (float)s.lo[a];
+        f.inv_w[a] = (float)(1.0 / s.width[a]);
+    }
+    return f;
+}
+
+__device__ __forceinline__ bool locate_f32(const mk_snapshot_view &s, const SnapF32 &sf, float x, float y, float z,
+                                           CellPosF &c) {
+    const float xs[3] = {x, y, z};
+    int b[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float u = (xs[a] - sf.lo[a]) * sf.inv_w[a];
+        if (!(u >= 0.0f && u < (float)s.nb[a])) return false;
+        b[a] = min((int)u, s.nb[a] - 1);
+    }
+    const int mb = __ldg(s.table + ((int64_t)b[2] * s.nb[1] + b[1]) * s.nb[0] + b[0]);
+    if (mb < 0) return false;
+    c.mb = mb;
+    const float4 g0 = __ldg(reinterpret_cast<const float4 *>(s.geom_f32) + 2 * (int64_t)mb);
+    const float4 g1 = __ldg(reinterpret_cast<const float4 *>(s.geom_f32) + 2 * (int64_t)mb + 1);
+    const float left[3] = {g0.x, g0.y, g0.z}, inv_dx[3] = {g0.w, g1.x, g1.y};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float t = (xs[a] - left[a]) * inv_dx[a] + 1.0f;  // ghost-shifted
+        const float fl = floorf(t);
+        int i = (int)fl;
+        float d = t - fl;
+        if (i < 0) { i = 0; d = 0.0f; }
+        if (i > s.n) { i = s.n; d = 1.0f; }
+        c.idx[a] = i;
+        c.del[a] = d;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void trilinear8_f32(const mk_snapshot_view &s, const CellPosF &c, float prim[8]) {
+    const int n2 = s.n + 2;
+    const int64_t sj = (int64_t)n2 * 8, sk = (int64_t)n2 * n2 * 8;
+    const float *base = s.blocks + ((((int64_t)c.mb * n2 + c.idx[2]) * n2 + c.idx[1]) * n2 + c.idx[0]) * 8;
+    float v[2][2][2][8];
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                const float *p = base + dk * sk + dj * sj + di * 8;
+                const float4 lo = ldg4(p), hi = ldg4(p + 4);
+                v[dk][dj][di][0] = lo.x; v[dk][dj][di][1] = lo.y; v[dk][dj][di][2] = lo.z; v[dk][dj][di][3] = lo.w;
+                v[dk][dj][di][4] = hi.x; v[dk][dj][di][5] = hi.y; v[dk][dj][di][6] = hi.z; v[dk][dj][di][7] = hi.w;
+            }
+    const float d1 = c.del[0], d2 = c.del[1], d3 = c.del[2];
+#pragma unroll
+    for (int p = 0; p < 8; p++) {
+        const float daa = fmaf(v[0][0][1][p] - v[0][0][0][p], d1, v[0][0][0][p]);
+        const float dab = fmaf(v[0][1][1][p] - v[0][1][0][p], d1, v[0][1][0][p]);
+        const float dba = fmaf(v[1][0][1][p] - v[1][0][0][p], d1, v[1][0][0][p]);
+        const float dbb = fmaf(v[1][1][1][p] - v[1][1][0][p], d1, v[1][1][0][p]);
+        const float da = fmaf(dab - daa, d2, daa);
+        const float db = fmaf(dbb - dba, d2, dba);
+        prim[p] = fmaf(db - da, d3, da);
+    }
+}
+
+struct FluidF32 {
+    float dens, u, cos_pitch, kdotu, b;
+};
+
+// fluid frame in float; returns the clamped cosine of the pitch angle (the
+// emission needs sin(pitch) = sqrt(1 - cos^2), not the angle)
+__device__ __forceinline__ FluidF32 fluid_frame_f32(const float prim[8], float x, float y, float z, const float k[4],
+                                                    float a, float cos_fallback) {
+    const KerrPoint<float> m = kerr_point(x, y, z, a);
+    const float f = m.f, l1 = m.l1, l2 = m.l2, l3 = m.l3;
+    const float alpha = rsqrtf(1.0f + f);
+    const float U1 = prim[1], U2 = prim[2], U3 = prim[3];
+    const float lU = l1 * U1 + l2 * U2 + l3 * U3;
+    const float gamma = sqrtf(1.0f + ((U1 * U1 + U2 * U2 + U3 * U3) + f * lU * lU));
+    const float ga_f = gamma * alpha * f;
+    const float uc0 = gamma / alpha;
+    const float uc1 = U1 - ga_f * l1, uc2 = U2 - ga_f * l2, uc3 = U3 - ga_f * l3;
+    const float lu = uc0 + l1 * uc1 + l2 * uc2 + l3 * uc3;
+    const float flu = f * lu;
+    const float ud0 = -uc0 + flu, ud1 = uc1 + l1 * flu, ud2 = uc2 + l2 * flu, ud3 = uc3 + l3 * flu;
+    const float B1 = prim[5], B2 = prim[6], B3 = prim[7];
+    const float bc0 = B1 * ud1 + B2 * ud2 + B3 * ud3;
+    const float iuc0 = 1.0f / uc0;
+    const float bc1 = (B1 + uc1 * bc0) * iuc0, bc2 = (B2 + uc2 * bc0) * iuc0, bc3 = (B3 + uc3 * bc0) * iuc0;
+    const float lb = bc0 + l1 * bc1 + l2 * bc2 + l3 * bc3;
+    const float flb = f * lb;
+    const float bd0 = -bc0 + flb, bd1 = bc1 + l1 * flb, bd2 = bc2 + l2 * flb, bd3 = bc3 + l3 * flb;
+    FluidF32 o;
+    o.kdotu = k[0] * ud0 + k[1] * ud1 + k[2] * ud2 + k[3] * ud3;
+    const float kdotb = k[0] * bd0 + k[1] * bd1 + k[2] * bd2 + k[3] * bd3;
+    const float bdotb = bc0 * bd0 + bc1 * bd1 + bc2 * bd2 + bc3 * bd3;
+    float cp = kdotb / (fabsf(o.kdotu) * sqrtf(bdotb));
+    if (isnan(cp)) cp = cos_fallback;
+    o.cos_pitch = fminf(fmaxf(cp, -1.0f), 1.0f);
+    o.dens = prim[0];
+    o.u = prim[4];
+    o.b = sqrtf(bdotb);
+    return o;
 }
 
 }  // namespace mk

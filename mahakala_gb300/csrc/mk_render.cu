@@ -1,4 +1,4 @@
-// mk_render.cu -- fused persistent render kernel (make_image, images.py:30-144).
+// mk_render.cu -- fused persistent render kernels (make_image, images.py:30-144).
 //
 // One CUDA thread owns one ray at a time.  Per accepted RK4 step it samples
 // the snapshot at the new point, evaluates the electron temperature and the
@@ -15,25 +15,57 @@
 // Work distribution: rays are handed out by a global atomic counter; when a
 // lane's ray finishes it takes the next ray (warp-aggregated atomics), so
 // warps stay full while rays of very different lengths finish.  Requests of
-// any size can share one launch: a ray index maps to its request by a binary
+// any size share one launch: a ray index maps to its request by a binary
 // search over the requests' ray offsets.
+//
+// Precision forms:
+//   MK_FP64  one launch, every operation in FP64 (the reference's x64).
+//   MK_MIXED three launches on the caller's stream:
+//     A  FP32 from the camera.  A ray whose radius drops below R_FP64 (3 M),
+//        or that moves inward inside R_TURN (6 M, where photon-ring rays
+//        reach their turning points), is handed to an FP64 queue;
+//     B  FP64 over that queue: the near-horizon steps and the turning point.
+//        On entry the wavevector is renormalised to null in FP64.  A ray
+//        that leaves R_TURN outward is handed to an FP32 queue;
+//     C  FP32 over the second queue until the ray stops.
+//   Splitting by precision keeps each warp uniform: on a part whose FP64
+//   rate is 1/64 of FP32, one FP64 lane would stall the other 31.  The
+//   intensity accumulates with a compensated (Kahan) FP32 sum and the
+//   transmission product in FP32; both move to FP64 with the ray.
 #include "mk_common.cuh"
 #include "mk_fluid.cuh"
 
 namespace mk {
 
 constexpr int RENDER_THREADS = 128;
+constexpr double R_FP64 = 3.0;
+constexpr double R_TURN = 6.0;
 
-// scratch of one launch: the ray counter and the work totals the launch
-// accumulates (accepted steps, in-snapshot samples) for throughput and
-// roofline accounting
+// launch scratch: counters and work totals, then (mixed form) two queues
 struct RenderWorkspace {
-    unsigned long long counter;
-    unsigned long long steps;
-    unsigned long long samples;
+    unsigned long long counter;       // next camera ray (phase A / FP64 form)
+    unsigned long long steps;         // accepted RK4 steps
+    unsigned long long samples;       // in-snapshot samples
     unsigned long long max_tau_bits;  // max per-step optical depth w*alpha (bits of a double >= 0)
-    int error;
-    int pad;
+    unsigned long long q64_count;     // rays handed to FP64
+    unsigned long long q64_next;
+    unsigned long long q32_count;     // rays handed back to FP32
+    unsigned long long q32_next;
+    unsigned long long steps_fp64;    // accepted steps taken in FP64 (mixed form)
+    unsigned long long overflow;      // queue overflow (cannot happen: capacity = rays)
+};
+constexpr size_t WS_HEADER = 256;
+static_assert(sizeof(RenderWorkspace) <= WS_HEADER, "workspace header");
+
+// a ray in flight between the precision phases
+struct RayRecord {
+    double s[8];
+    double I[MK_MAX_NU];
+    double P[MK_MAX_NU];
+    double max_tau;
+    long long ray;
+    int steps, nsamples;
+    int rq, pad;
 };
 
 __device__ __forceinline__ int find_request(const mk_request *__restrict__ reqs, int nreq, long long ray) {
@@ -50,6 +82,43 @@ __device__ __forceinline__ int64_t request_pixels(const mk_camera &c) {
     return c.kind == MK_CAMERA_EQUATOR ? (int64_t)c.pixels : (int64_t)c.pixels * c.pixels;
 }
 
+// warp-aggregated work fetch: returns this lane's item index, -1 when the
+// lane asked and the work is exhausted, -2 when the lane did not ask
+__device__ __forceinline__ long long fetch(bool want, unsigned long long *counter, long long total) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned need = __ballot_sync(FULL, want);
+    if (!need) return -2;
+    const int leader = __ffs(need) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(need));
+    base = __shfl_sync(FULL, base, leader);
+    if (!want) return -2;
+    const long long idx = (long long)base + __popc(need & ((1u << lane) - 1u));
+    return idx < total ? idx : -1;
+}
+
+__device__ __forceinline__ void record_tau(RenderWorkspace *ws, double max_tau) {
+    // explicit Euler transfer is stable while every step has w*alpha < 1;
+    // non-negative doubles order like their bit patterns
+    if (max_tau > 0.0) atomicMax(&ws->max_tau_bits, (unsigned long long)__double_as_longlong(max_tau));
+}
+
+template <typename T>
+__device__ __forceinline__ void finish_ray(const mk_request &R, int64_t pix, const T I[MK_MAX_NU], int steps,
+                                           int why, int nsamples, double max_tau, RenderWorkspace *ws) {
+    const int64_t npx = request_pixels(R.camera);
+    if (steps) atomicAdd(&ws->steps, (unsigned long long)steps);
+    if (nsamples) atomicAdd(&ws->samples, (unsigned long long)nsamples);
+    record_tau(ws, max_tau);
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++)
+        if (ch < R.nnu) R.image[ch * npx + pix] = (double)I[ch];
+    if (R.nsteps) R.nsteps[pix] = steps;
+    if (R.status) R.status[pix] = why;
+}
+
+// ------------------------------------------------------------------ FP64
 // One sample of the emission at state s after a step of size dt_used,
 // folded into (I, P) for each frequency.  Returns without touching I, P
 // outside the snapshot, where the reference's zeroed primitives give
@@ -87,78 +156,90 @@ __device__ __forceinline__ void sample_fp64(const mk_request &R, const mk_snapsh
     }
 }
 
-__device__ __forceinline__ void finish_ray(const mk_request &R, int64_t pix, const double I[MK_MAX_NU], int steps,
-                                           int why, int nsamples, double max_tau, RenderWorkspace *ws) {
-    const int64_t npx = request_pixels(R.camera);
-    // explicit Euler transfer is stable while every step has w*alpha < 1;
-    // the launch records its largest value (non-negative doubles order like
-    // their bit patterns)
-    if (max_tau > 0.0) atomicMax(&ws->max_tau_bits, (unsigned long long)__double_as_longlong(max_tau));
-    if (steps) atomicAdd(&ws->steps, (unsigned long long)steps);
-    if (nsamples) atomicAdd(&ws->samples, (unsigned long long)nsamples);
-#pragma unroll
-    for (int ch = 0; ch < MK_MAX_NU; ch++)
-        if (ch < R.nnu) R.image[ch * npx + pix] = I[ch];
-    if (R.nsteps) R.nsteps[pix] = steps;
-    if (R.status) R.status[pix] = why;
+// Rescale k^t so that g(k, k) = 0 at x, keeping the spatial wavevector:
+// g00 k0^2 + 2 g0i k^i k0 + gij k^i k^j = 0, the root nearest the current k0.
+__device__ __forceinline__ void renull_fp64(double s[8], double a) {
+    const KerrPoint<double> m = kerr_point(s[1], s[2], s[3], a);
+    const double f = m.f;
+    const double lk = m.l1 * s[5] + m.l2 * s[6] + m.l3 * s[7];
+    const double A = -1.0 + f;                      // g00
+    const double B = 2.0 * f * lk;                  // 2 g0i k^i
+    const double C = s[5] * s[5] + s[6] * s[6] + s[7] * s[7] + f * lk * lk;
+    const double disc = B * B - 4.0 * A * C;
+    if (!(disc >= 0.0) || A == 0.0) return;
+    const double sq = sqrt(disc);
+    const double r1 = (-B + sq) / (2.0 * A), r2 = (-B - sq) / (2.0 * A);
+    s[4] = fabs(r1 - s[4]) < fabs(r2 - s[4]) ? r1 : r2;
 }
 
+enum { SRC_CAMERA = 0, SRC_QUEUE = 1 };
+
+// FP64 render.  SRC_CAMERA: every ray of the job, start to end (MK_FP64).
+// SRC_QUEUE: mixed-form phase B over the FP64 queue; rays leaving R_TURN
+// outward go to the FP32 queue.
+template <int SRC>
 __global__ void __launch_bounds__(RENDER_THREADS)
-render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long total,
-                   const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws) {
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const unsigned lt_mask = (1u << lane) - 1u;
+render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
+                   const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64,
+                   RayRecord *q32, long long capacity) {
+    unsigned long long *counter = SRC == SRC_CAMERA ? &ws->counter : &ws->q64_next;
+    const long long total =
+        SRC == SRC_CAMERA ? total_camera : (long long)*(volatile unsigned long long *)&ws->q64_count;
     bool active = false, exhausted = false;
-    int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE;
-    double max_tau = 0.0;
+    int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE, fp64_steps = 0;
+    long long ray = 0;
     int64_t pix = 0;
-    double s[8], dt = 0.0, I[MK_MAX_NU], P[MK_MAX_NU];
+    double s[8], dt = 0.0, r_cur = 0.0, I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0;
 
     for (;;) {
-        const unsigned need = __ballot_sync(FULL, !active && !exhausted);
-        if (need) {
-            const int leader = __ffs(need) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(&ws->counter, (unsigned long long)__popc(need));
-            base = __shfl_sync(FULL, base, leader);
-            if (!active && !exhausted) {
-                const long long idx = (long long)base + __popc(need & lt_mask);
-                if (idx < total) {
-                    rq = find_request(reqs, nreq, idx);
-                    const mk_request &R = reqs[rq];
-                    pix = idx - R.ray_offset;
-                    camera_ray(R.camera, pix, s);
-                    steps = 0;
-                    nsamples = 0;
-                    max_tau = 0.0;
+        const long long idx = fetch(!active && !exhausted, counter, total);
+        if (idx == -1) exhausted = true;
+        if (idx >= 0) {
+            if (SRC == SRC_CAMERA) {
+                ray = idx;
+                rq = find_request(reqs, nreq, ray);
+                pix = ray - reqs[rq].ray_offset;
+                camera_ray(reqs[rq].camera, pix, s);
+                steps = nsamples = 0;
+                max_tau = 0.0;
 #pragma unroll
-                    for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = 0.0; P[ch] = 1.0; }
-                    const double a = R.camera.bhspin;
-                    dt = reference_dt(radius_cal(s[1], s[2], s[3], a), radius_eh(a), R.policy.div,
-                                      R.policy.tol, why);
-                    if (dt == 0.0 || R.policy.nmax < 2) {
-                        // stopped before its first step (reference K = 0), or
-                        // N < 2 leaves no row pair for the transfer solve
-                        if (why == MK_RAY_ACTIVE) why = MK_RAY_MAXSTEPS;
-                        finish_ray(R, pix, I, 0, why, 0, 0.0, ws);
-                    } else {
-                        active = true;
-                    }
-                } else {
-                    exhausted = true;
-                }
+                for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = 0.0; P[ch] = 1.0; }
+            } else {
+                const RayRecord &q = q64[idx];
+#pragma unroll
+                for (int i = 0; i < 8; i++) s[i] = q.s[i];
+#pragma unroll
+                for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = q.I[ch]; P[ch] = q.P[ch]; }
+                max_tau = q.max_tau;
+                ray = q.ray;
+                steps = q.steps;
+                nsamples = q.nsamples;
+                rq = q.rq;
+                pix = ray - reqs[rq].ray_offset;
+                renull_fp64(s, reqs[rq].camera.bhspin);
+            }
+            const mk_request &R = reqs[rq];
+            const double a = R.camera.bhspin;
+            r_cur = radius_cal(s[1], s[2], s[3], a);
+            dt = reference_dt(r_cur, radius_eh(a), R.policy.div, R.policy.tol, why);
+            if (dt == 0.0 || R.policy.nmax < 2) {
+                // stopped before its next step (reference K = steps), or N < 2
+                // leaves no row pair for the transfer solve
+                if (why == MK_RAY_ACTIVE) why = MK_RAY_MAXSTEPS;
+                finish_ray(R, pix, I, steps, why, nsamples, max_tau, ws);
+            } else {
+                active = true;
             }
         }
-        if (!__any_sync(FULL, active)) break;
+        if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
             const mk_request &R = reqs[rq];
             const double a = R.camera.bhspin;
             double nw[8];
             rk4_step(s, dt, a, nw);
             int w1;
-            const double dtn = reference_dt(radius_cal(nw[1], nw[2], nw[3], a), radius_eh(a), R.policy.div,
-                                            R.policy.tol, w1);
+            const double r_new = radius_cal(nw[1], nw[2], nw[3], a);
+            const double dtn = reference_dt(r_new, radius_eh(a), R.policy.div, R.policy.tol, w1);
             if (dtn == 0.0) {
                 // the step is rejected and the ray stays frozen (geodesics.py:263-267)
                 finish_ray(R, pix, I, steps, w1, nsamples, max_tau, ws);
@@ -169,53 +250,291 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
                 const double dt_used = dt;
                 dt = dtn;
                 ++steps;
+                ++fp64_steps;
                 sample_fp64(R, snaps[R.snapshot], s, dt_used, I, P, nsamples, max_tau);
                 // trajectory rows stop at N-1: step N-1 never reaches the solve
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray(R, pix, I, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
                     active = false;
+                } else if (SRC == SRC_QUEUE && r_new >= R_TURN && r_new > r_cur) {
+                    // outbound past the photon-ring region: back to FP32
+                    const unsigned long long slot = atomicAdd(&ws->q32_count, 1ull);
+                    if ((long long)slot < capacity) {
+                        RayRecord &q = q32[slot];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) q.s[i] = s[i];
+#pragma unroll
+                        for (int ch = 0; ch < MK_MAX_NU; ch++) { q.I[ch] = I[ch]; q.P[ch] = P[ch]; }
+                        q.max_tau = max_tau;
+                        q.ray = ray;
+                        q.steps = steps;
+                        q.nsamples = nsamples;
+                        q.rq = rq;
+                        active = false;
+                    } else {
+                        atomicAdd(&ws->overflow, 1ull);  // keep integrating in FP64
+                    }
                 }
+                r_cur = r_new;
+            }
+        }
+    }
+    if (SRC == SRC_QUEUE && fp64_steps) atomicAdd(&ws->steps_fp64, (unsigned long long)fp64_steps);
+}
+
+// ------------------------------------------------------------------ FP32
+// emission of one sample in float (mixed form); I is a compensated sum
+__device__ __forceinline__ void sample_f32(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
+                                           const float s[8], float dt_used, float a, float I[MK_MAX_NU],
+                                           float Ic[MK_MAX_NU], float P[MK_MAX_NU], const SynchroF32 sc[MK_MAX_NU],
+                                           int &nsamples, float &max_tau) {
+    CellPosF c;
+    if (!locate_f32(sv, sf, s[1], s[2], s[3], c)) return;
+    ++nsamples;
+    float prim[8];
+    trilinear8_f32(sv, c, prim);
+    const FluidF32 fs = fluid_frame_f32(prim, s[1], s[2], s[3], s + 4, a, (float)R.cos_fallback_pitch);
+    const float bsq = fs.b * fs.b;
+    const float beta = fs.u * (float)(R.fluid_gamma - 1.) / bsq * 2.0f;
+    const float sigma = bsq / fs.dens;
+    const float b2 = beta * beta;
+    const float T_ratio = ((float)R.r_high * b2 + (float)R.r_low) / (1.0f + b2);
+    const float gem1 = (float)R.electron_gamma_m1, gim1 = (float)R.ion_gamma_m1;
+    // Theta_e = (MP/ME) u gem1 gim1 / (dens (gim1 + gem1 T_ratio))
+    const float Th = (float)(MP / ME) * fs.u * gem1 * gim1 / (fs.dens * (gim1 + gem1 * T_ratio));
+    const float Ne = (float)R.Ne_unit * fs.dens;
+    const float Bg = (float)R.B_unit * fs.b;
+    const float sin_p = sqrtf(fmaxf(0.0f, 1.0f - fs.cos_pitch * fs.cos_pitch));
+    const float th2 = Th * Th;
+    // nus in Hz; nu' = -k.u (observed frequency rescaled to 1)
+    const float nus = (float)(TWO_NINTHS * EE / TWO_PI_ME_CL) * Bg * th2 * sin_p;
+    const float nup = -fs.kdotu;
+    const float w = -dt_used * (float)R.L_unit;
+    const bool cut = sigma > (float)R.sigma_cut || Th < 0.3f;
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++) {
+        if (ch < R.nnu) {
+            const float nusp = nus * sc[ch].inv_nu;  // nus / nu_obs
+            const float X = nup / nusp;
+            const float x3 = cbrtf(X);
+            const float term = sqrtf(X) + (float)C2_11_12 * sqrtf(x3);
+            // emissivity / nu'^2 (invariant, rescaled): k_em folds
+            // sqrt2 pi EE^2 / (3 CL) and nu_obs
+            float em = Ne * sc[ch].k_em * nusp * term * term / (2.0f * th2) * __expf(-x3) / (nup * nup);
+            if (X > 1.e12f || cut) em = 0.0f;
+            const float bx = sc[ch].k_bx * nup / Th;
+            const float bden = bx < 2.e-3f ? bx / 24.f * (24.f + bx * (12.f + bx * (4.f + bx))) : expm1f(bx);
+            // alpha nu' = (em nu'^2) / B_nu * nu' with B_nu = k_bnu nu'^3 / bden
+            float ab = em * bden / sc[ch].k_bnu;
+            if (isnan(em)) em = 0.0f;
+            if (isnan(ab)) ab = 0.0f;
+            const float tau = w * ab;
+            // Kahan-compensated I += (w em) P
+            const float y = (w * em) * P[ch] - Ic[ch];
+            const float t = I[ch] + y;
+            Ic[ch] = (t - I[ch]) - y;
+            I[ch] = t;
+            P[ch] *= (1.0f - tau);
+            max_tau = fmaxf(max_tau, tau);
+        }
+    }
+}
+
+__device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix, const float I[MK_MAX_NU],
+                                               const float Ic[MK_MAX_NU], int steps, int why, int nsamples,
+                                               float max_tau, RenderWorkspace *ws) {
+    double Iout[MK_MAX_NU];
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++) Iout[ch] = (double)I[ch] - (double)Ic[ch];
+    finish_ray(R, pix, Iout, steps, why, nsamples, (double)max_tau, ws);
+}
+
+// FP32 render phase.  SRC_CAMERA: mixed-form phase A from the camera, with
+// hand-off to the FP64 queue.  SRC_QUEUE: phase C over the FP32 queue.
+template <int SRC>
+__global__ void __launch_bounds__(RENDER_THREADS)
+render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
+                  const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64, RayRecord *q32,
+                  long long capacity) {
+    unsigned long long *counter = SRC == SRC_CAMERA ? &ws->counter : &ws->q32_next;
+    const long long total =
+        SRC == SRC_CAMERA ? total_camera : (long long)*(volatile unsigned long long *)&ws->q32_count;
+    bool active = false, exhausted = false;
+    int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE;
+    long long ray = 0;
+    int64_t pix = 0;
+    float s[8], dt = 0.0f, r_cur = 0.0f, reh = 0.0f, a = 0.0f, max_tau = 0.0f;
+    float I[MK_MAX_NU], Ic[MK_MAX_NU], P[MK_MAX_NU];
+    SynchroF32 sc[MK_MAX_NU];
+    SnapF32 sf;
+
+    for (;;) {
+        const long long idx = fetch(!active && !exhausted, counter, total);
+        if (idx == -1) exhausted = true;
+        if (idx >= 0) {
+            double s64[8];
+            if (SRC == SRC_CAMERA) {
+                ray = idx;
+                rq = find_request(reqs, nreq, ray);
+                pix = ray - reqs[rq].ray_offset;
+                camera_ray(reqs[rq].camera, pix, s64);
+                steps = nsamples = 0;
+                max_tau = 0.0f;
+#pragma unroll
+                for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = 0.0f; Ic[ch] = 0.0f; P[ch] = 1.0f; }
+            } else {
+                const RayRecord &q = q32[idx];
+#pragma unroll
+                for (int i = 0; i < 8; i++) s64[i] = q.s[i];
+#pragma unroll
+                for (int ch = 0; ch < MK_MAX_NU; ch++) {
+                    I[ch] = (float)q.I[ch];
+                    Ic[ch] = (float)((double)I[ch] - q.I[ch]);
+                    P[ch] = (float)q.P[ch];
+                }
+                max_tau = (float)q.max_tau;
+                ray = q.ray;
+                steps = q.steps;
+                nsamples = q.nsamples;
+                rq = q.rq;
+                pix = ray - reqs[rq].ray_offset;
+                renull_fp64(s64, reqs[rq].camera.bhspin);
+            }
+            const mk_request &R = reqs[rq];
+#pragma unroll
+            for (int i = 0; i < 8; i++) s[i] = (float)s64[i];
+            a = (float)R.camera.bhspin;
+            reh = (float)radius_eh(R.camera.bhspin);
+#pragma unroll
+            for (int ch = 0; ch < MK_MAX_NU; ch++)
+                if (ch < R.nnu) sc[ch] = synchro_consts(R.nu[ch]);
+            sf = snap_f32(snaps[R.snapshot]);
+            r_cur = radius_cal(s[1], s[2], s[3], a);
+            dt = reference_dt(r_cur, reh, (float)R.policy.div, (float)R.policy.tol, why);
+            if (dt == 0.0f || R.policy.nmax < 2) {
+                if (why == MK_RAY_ACTIVE) why = MK_RAY_MAXSTEPS;
+                finish_ray_f32(R, pix, I, Ic, steps, why, nsamples, max_tau, ws);
+            } else {
+                active = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) {
+            const mk_request &R = reqs[rq];
+            float nw[8];
+            rk4_step(s, dt, a, nw);
+            int w1;
+            const float r_new = radius_cal(nw[1], nw[2], nw[3], a);
+            const float dtn = reference_dt(r_new, reh, (float)R.policy.div, (float)R.policy.tol, w1);
+            if (dtn == 0.0f) {
+                finish_ray_f32(R, pix, I, Ic, steps, w1, nsamples, max_tau, ws);
+                active = false;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; i++) s[i] = nw[i];
+                const float dt_used = dt;
+                dt = dtn;
+                ++steps;
+                sample_f32(R, snaps[R.snapshot], sf, s, dt_used, a, I, Ic, P, sc, nsamples, max_tau);
+                if (steps >= R.policy.nmax - 1) {
+                    finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
+                    active = false;
+                } else if (SRC == SRC_CAMERA &&
+                           (r_new < (float)R_FP64 || (r_new < (float)R_TURN && r_new < r_cur))) {
+                    // near the horizon or inbound in the photon-ring region: FP64
+                    const unsigned long long slot = atomicAdd(&ws->q64_count, 1ull);
+                    if ((long long)slot < capacity) {
+                        RayRecord &q = q64[slot];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) q.s[i] = (double)s[i];
+#pragma unroll
+                        for (int ch = 0; ch < MK_MAX_NU; ch++) {
+                            q.I[ch] = (double)I[ch] - (double)Ic[ch];
+                            q.P[ch] = (double)P[ch];
+                        }
+                        q.max_tau = (double)max_tau;
+                        q.ray = ray;
+                        q.steps = steps;
+                        q.nsamples = nsamples;
+                        q.rq = rq;
+                        active = false;
+                    } else {
+                        atomicAdd(&ws->overflow, 1ull);
+                    }
+                }
+                r_cur = r_new;
             }
         }
     }
 }
 
-static int blocks_per_sm_fp64() {
-    static int cached[64] = {0};
+template <typename K>
+static int blocks_per_sm(K kernel, int slot) {
+    static int cached[64][4] = {{0}};
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 64 && cached[dev]) return cached[dev];
+    if (dev < 64 && cached[dev][slot]) return cached[dev][slot];
     int nb = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, render_fp64_kernel, RENDER_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, RENDER_THREADS, 0);
     if (nb < 1) nb = 1;
-    if (dev < 64) cached[dev] = nb;
+    if (dev < 64) cached[dev][slot] = nb;
     return nb;
+}
+
+static unsigned persistent_grid(int per_sm, int64_t rays) {
+    int64_t grid = (int64_t)device_sm_count() * per_sm;
+    const int64_t need = (rays + RENDER_THREADS - 1) / RENDER_THREADS;
+    if (grid > need) grid = need;
+    return (unsigned)(grid < 1 ? 1 : grid);
 }
 
 }  // namespace mk
 
 using namespace mk;
 
-extern "C" size_t mk_render_workspace_bytes(void) { return 256; }
+extern "C" size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision) {
+    if (total_rays < 0) return 0;
+    if (precision == MK_MIXED) return WS_HEADER + 2 * (size_t)total_rays * sizeof(RayRecord);
+    return WS_HEADER;
+}
 
 extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
                          const mk_snapshot_view *snaps_dev, int32_t nsnap, int32_t precision,
                          void *workspace_dev, size_t workspace_bytes, void *stream) {
     MK_REQUIRE(reqs_dev && snaps_dev && workspace_dev, MK_ERR_ARG, "mk_render: null pointer");
     MK_REQUIRE(nreq > 0 && nsnap > 0 && total_rays >= 0, MK_ERR_ARG, "mk_render: bad sizes");
-    MK_REQUIRE(workspace_bytes >= mk_render_workspace_bytes(), MK_ERR_ARG,
-               "mk_render: workspace of %zu bytes, need %zu", workspace_bytes, mk_render_workspace_bytes());
-    MK_REQUIRE(((uintptr_t)workspace_dev & 7) == 0, MK_ERR_ARG, "mk_render: workspace not 8-byte aligned");
-    MK_REQUIRE(precision == MK_FP64, MK_ERR_UNSUPPORTED, "mk_render: precision %d not built", (int)precision);
+    MK_REQUIRE(precision == MK_FP64 || precision == MK_MIXED, MK_ERR_ARG, "mk_render: unknown precision %d",
+               (int)precision);
+    const size_t need = mk_render_workspace_bytes(total_rays, precision);
+    MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render: workspace of %zu bytes, need %zu",
+               workspace_bytes, need);
+    MK_REQUIRE(((uintptr_t)workspace_dev & 15) == 0, MK_ERR_ARG, "mk_render: workspace not 16-byte aligned");
     cudaStream_t st = as_stream(stream);
-    MK_CUDA(cudaMemsetAsync(workspace_dev, 0, sizeof(RenderWorkspace), st));
+    MK_CUDA(cudaMemsetAsync(workspace_dev, 0, WS_HEADER, st));
     if (total_rays == 0) return MK_OK;
-    const int64_t warps = (total_rays + 31) / 32;
-    int64_t grid = (int64_t)device_sm_count() * blocks_per_sm_fp64();
-    const int64_t need = (warps * 32 + RENDER_THREADS - 1) / RENDER_THREADS;
-    if (grid > need) grid = need;
-    render_fp64_kernel<<<(unsigned)grid, RENDER_THREADS, 0, st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev,
-                                                                  (RenderWorkspace *)workspace_dev);
-    MK_LAUNCHED("render_fp64_kernel");
+    RenderWorkspace *ws = (RenderWorkspace *)workspace_dev;
+    if (precision == MK_FP64) {
+        const unsigned grid = persistent_grid(blocks_per_sm(render_fp64_kernel<SRC_CAMERA>, 0), total_rays);
+        render_fp64_kernel<SRC_CAMERA><<<grid, RENDER_THREADS, 0, st>>>(reqs_dev, nreq, (long long)total_rays,
+                                                                        snaps_dev, ws, nullptr, nullptr, 0);
+        MK_LAUNCHED("render_fp64_kernel");
+        return MK_OK;
+    }
+    RayRecord *q64 = (RayRecord *)((char *)workspace_dev + WS_HEADER);
+    RayRecord *q32 = q64 + total_rays;
+    const long long cap = (long long)total_rays;
+    render_f32_kernel<SRC_CAMERA>
+        <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA>, 1), total_rays), RENDER_THREADS, 0, st>>>(
+            reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap);
+    MK_LAUNCHED("render_f32_kernel (camera)");
+    // the queues' sizes are only known on the device: full persistent grids
+    render_fp64_kernel<SRC_QUEUE>
+        <<<persistent_grid(blocks_per_sm(render_fp64_kernel<SRC_QUEUE>, 2), total_rays), RENDER_THREADS, 0, st>>>(
+            reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
+    MK_LAUNCHED("render_fp64_kernel (queue)");
+    render_f32_kernel<SRC_QUEUE>
+        <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE>, 3), total_rays), RENDER_THREADS, 0, st>>>(
+            reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
+    MK_LAUNCHED("render_f32_kernel (queue)");
     return MK_OK;
 }

@@ -54,6 +54,17 @@ __global__ void snapshot_build_kernel(const float *__restrict__ uov, const float
     }
 }
 
+// float copy of the per-block geometry for the mixed-precision sampler:
+// (x1v[0], x2v[0], x3v[0], 1/dx1, 1/dx2, 1/dx3, 0, 0) per block
+__global__ void geom_f32_kernel(const double *__restrict__ geom, int nmb, float *__restrict__ out) {
+    const int mb = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mb >= nmb) return;
+    const double *g = geom + 6 * (int64_t)mb;
+    float4 *o = reinterpret_cast<float4 *>(out + 8 * (int64_t)mb);
+    o[0] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)(1.0 / g[3]));
+    o[1] = make_float4((float)(1.0 / g[4]), (float)(1.0 / g[5]), 0.0f, 0.0f);
+}
+
 __global__ void fluid_scalars_kernel(mk_snapshot_view sv, double a, const double *__restrict__ S, int64_t npts,
                                      double cos_fallback, double *__restrict__ out) {
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -149,10 +160,14 @@ __global__ void attenuated_kernel(const double *__restrict__ em, const double *_
 
 using namespace mk;
 
-extern "C" size_t mk_snapshot_bytes(int32_t nmb, int32_t n) {
-    if (nmb <= 0 || n <= 0) return 0;
+static size_t blocks_bytes(int32_t nmb, int32_t n) {
     const size_t n2 = (size_t)n + 2;
     return (size_t)nmb * n2 * n2 * n2 * 8 * sizeof(float);
+}
+
+extern "C" size_t mk_snapshot_bytes(int32_t nmb, int32_t n) {
+    if (nmb <= 0 || n <= 0) return 0;
+    return blocks_bytes(nmb, n) + (size_t)nmb * 8 * sizeof(float);
 }
 
 extern "C" int mk_snapshot_build(const float *uov_dev, const float *B_dev, const int32_t *locs_dev,
@@ -176,9 +191,13 @@ extern "C" int mk_snapshot_build(const float *uov_dev, const float *B_dev, const
     snapshot_build_kernel<<<(unsigned)grid, 256, 0, as_stream(stream)>>>(uov_dev, B_dev, locs_dev, table_dev, nmb, n,
                                                                        nb[0], nb[1], nb[2], (float *)storage_dev);
     MK_LAUNCHED("snapshot_build_kernel");
+    float *gf = (float *)((char *)storage_dev + blocks_bytes(nmb, n));
+    geom_f32_kernel<<<grid_for(nmb, 128), 128, 0, as_stream(stream)>>>(geom_dev, nmb, gf);
+    MK_LAUNCHED("geom_f32_kernel");
     mk_snapshot_view v;
     v.blocks = (const float *)storage_dev;
     v.geom = geom_dev;
+    v.geom_f32 = gf;
     v.faces = faces_dev;
     v.table = table_dev;
     v.nmb = nmb;

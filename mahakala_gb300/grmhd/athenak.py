@@ -106,7 +106,7 @@ class DeviceSnapshot:
     def blocks(self):
         """(nmb, n+2, n+2, n+2, 8) float32 view of the resident meshblocks."""
         n2 = self.n + 2
-        return self.storage.view(self.nmb, n2, n2, n2, 8)
+        return self.storage[: self.nmb * n2 ** 3 * 8].view(self.nmb, n2, n2, n2, 8)
 
 
 class AthenakFluidModel(GRMHDFluidModel):

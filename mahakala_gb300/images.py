@@ -117,7 +117,8 @@ class PreparedRender:
         self.reqs_dev = torch.frombuffer(bytearray(self.table_bytes), dtype=torch.uint8).to(dev)
         self.snaps_dev = torch.cat([sn.view_dev for sn in snaps]) if len(snaps) > 1 else snaps[0].view_dev
         self.nsnap = len(snaps)
-        self.ws = torch.zeros(_lib.load().mk_render_workspace_bytes() // 8, dtype=torch.int64, device=dev)
+        nbytes = _lib.load().mk_render_workspace_bytes(self.total_rays, self.precision)
+        self.ws = torch.zeros((nbytes + 7) // 8, dtype=torch.int64, device=dev)
 
     def launch(self, stream=None):
         _lib.call("mk_render", ptr(self.reqs_dev), len(self.requests), self.total_rays, ptr(self.snaps_dev),
@@ -126,13 +127,19 @@ class PreparedRender:
 
     def work_totals(self):
         """(accepted steps, in-snapshot samples) of the last launch (syncs)."""
-        w = self.ws.cpu()
+        w = self.ws[:32].cpu()
         return int(w[_lib.MK_WS_STEPS]), int(w[_lib.MK_WS_SAMPLES])
+
+    def precision_split(self):
+        """(rays handed to FP64, rays handed back to FP32, steps taken in
+        FP64) of the last mixed-form launch (syncs)."""
+        w = self.ws[:32].cpu()
+        return int(w[_lib.MK_WS_TO_FP64]), int(w[_lib.MK_WS_TO_FP32]), int(w[_lib.MK_WS_STEPS_FP64])
 
     def max_step_optical_depth(self):
         """Largest per-step w*alpha of the last launch (syncs); the explicit
         Euler transfer of the reference is stable while this stays below 1."""
-        return float(self.ws.cpu()[_lib.MK_WS_MAX_TAU:_lib.MK_WS_MAX_TAU + 1].view(torch.float64)[0])
+        return float(self.ws[:32].cpu()[_lib.MK_WS_MAX_TAU:_lib.MK_WS_MAX_TAU + 1].view(torch.float64)[0])
 
 
 def render_requests(requests, precision="fp64", stream=None, with_steps=False):

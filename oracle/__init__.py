@@ -193,14 +193,16 @@ def perturbed(s0, eps=1e-12):
     return s
 
 
-def ill_conditioned(state, state_pert, eps=1e-12, amplification=100.0, floor=1e-3):
-    """Rays whose end state moves by more than amplification*eps (relative,
-    floor 1e-3) when the initial wavevector moves by eps: photon-ring rays
-    whose end state no FP64 evaluation order reproduces to the parity bar."""
+def amplification(state, state_pert, eps=1e-12, floor=1e-3):
+    """Per ray: relative end-state change (floor 1e-3 for components near
+    zero) per unit relative change eps of the initial wavevector.  Rounding
+    differences of two FP64 evaluation orders (~1e-13 accumulated over a
+    ray) reach the end state multiplied by this factor; rays near the
+    critical curve reach 1e5 and more."""
     with np.errstate(all="ignore"):
         d = np.abs(state - state_pert) / np.maximum(np.abs(state), floor)
     d = np.where(np.isnan(d), np.inf, d)
-    return d.reshape(d.shape[0], -1).max(axis=1) > amplification * eps
+    return d.reshape(d.shape[0], -1).max(axis=1) / eps
 
 
 def trimmed_rows(K, N):

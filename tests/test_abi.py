@@ -53,8 +53,9 @@ def test_struct_layouts(lib):
 def test_version_and_workspace(lib):
     assert lib.mk_abi_version() == 1
     assert b"sm_103a" in lib.mk_version()
-    assert lib.mk_render_workspace_bytes() >= 16
-    assert lib.mk_snapshot_bytes(8, 8) == 8 * 10 ** 3 * 32
+    assert lib.mk_render_workspace_bytes(100, 0) == 256
+    assert lib.mk_render_workspace_bytes(100, 1) > 256 + 2 * 100 * 100
+    assert lib.mk_snapshot_bytes(8, 8) == 8 * 10 ** 3 * 32 + 8 * 32
 
 
 def test_argument_errors_without_gpu(lib):

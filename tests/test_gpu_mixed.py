@@ -1,0 +1,75 @@
+"""Mixed-precision render (FP32 with FP64 near the hole and at the photon
+ring) against the FP64 render of the same request.
+
+Bar: total-flux relative error <= 1e-3 and max per-pixel relative error
+<= 1e-2 (floor 1e-4 of the image maximum), captured masks (shadow) equal
+to within a pixel ring, on every tested image.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FLUX_TOL = 1e-3
+PIX_TOL = 1e-2
+
+
+@pytest.fixture(scope="module")
+def medium_model():
+    from mahakala_gb300.grmhd.athenak import AthenakFluidModel
+    from mahakala_gb300.grmhd.synthetic import make_synthetic_snapshot
+    arrs = make_synthetic_snapshot(nblocks=4, cells_per_block=16, extent=50.0, bhspin=0.94, seed=11)
+    return AthenakFluidModel(arrs, 0.94, fluid_gamma=13. / 9)
+
+
+def _pair(model, **kw):
+    from mahakala_gb300.images import RenderRequest, render_requests
+    r64 = RenderRequest(model, **kw)
+    rmx = RenderRequest(model, **kw)
+    i64 = render_requests([r64], precision="fp64", with_steps=True)[0].cpu().numpy()
+    imx = render_requests([rmx], precision="mixed", with_steps=True)[0].cpu().numpy()
+    return i64, imx, r64.out["status"].cpu().numpy(), rmx.out["status"].cpu().numpy()
+
+
+@pytest.mark.parametrize("spin,inc,rh", [(0.94, 17.0, 40.0), (0.5, 60.0, 10.0), (0.0, 85.0, 1.0)])
+def test_mixed_matches_fp64(cuda, medium_model, spin, inc, rh):
+    from mahakala_gb300 import configs, metrics
+    kw = dict(camera_inclination=inc, mass_scale=configs.mass_scale_for(rh), M_bh=6.5e9 * 1.989e33, r_high=rh,
+              observing_frequency=230e9, fov=50.0, resolution=48, max_nsteps=8192, bhspin=spin)
+    i64, imx, s64, smx = _pair(medium_model, **kw)
+    assert i64.max() > 0 and np.all(np.isfinite(imx))
+    m = metrics.compare(imx, i64, smx, s64, 50.0)
+    print(spin, inc, rh, m)
+    assert m["flux_rel_err"] <= FLUX_TOL
+    assert m["max_pixel_rel_err"] <= PIX_TOL
+    assert abs(m["shadow_diameter"] - m["shadow_diameter_fp64"]) <= 2 * 50.0 / 48
+
+
+def test_mixed_multifrequency_and_batch(cuda, medium_model):
+    """Three frequencies in one mixed pass, and a batch of requests, each
+    within the bar of its FP64 render."""
+    from mahakala_gb300 import configs, metrics
+    from mahakala_gb300.images import RenderRequest, render_requests
+    kws = [dict(camera_inclination=30.0, observing_frequency=[86e9, 230e9, 345e9], resolution=32, fov=50.0,
+                mass_scale=configs.mass_scale_for(40.0), r_high=40.0, max_nsteps=8192),
+           dict(camera_inclination=70.0, observing_frequency=345e9, resolution=24, fov=40.0, bhspin=0.5,
+                mass_scale=configs.mass_scale_for(5.0), r_high=5.0, max_nsteps=8192)]
+    mixed = render_requests([RenderRequest(medium_model, **k) for k in kws], precision="mixed")
+    for k, imx in zip(kws, mixed):
+        i64 = render_requests([RenderRequest(medium_model, **k)], precision="fp64")[0].cpu().numpy()
+        imx = imx.cpu().numpy()
+        for c in range(i64.shape[0]):
+            assert metrics.flux_rel_err(imx[c], i64[c]) <= FLUX_TOL
+            assert metrics.max_pixel_rel_err(imx[c], i64[c]) <= PIX_TOL
+
+
+def test_mixed_hands_rays_to_fp64(cuda, medium_model):
+    """Captured rays and photon-ring rays are integrated in FP64 near the hole."""
+    from mahakala_gb300.images import PreparedRender, RenderRequest
+    prep = PreparedRender([RenderRequest(medium_model, camera_inclination=17.0, resolution=32, fov=50.0,
+                                         max_nsteps=8192)], precision="mixed")
+    prep.launch()
+    to64, back32, steps64 = prep.precision_split()
+    steps, _ = prep.work_totals()
+    assert to64 > 0 and back32 > 0 and 0 < steps64 < steps

@@ -60,14 +60,12 @@ def test_integrator_matches_oracle_many_rays(cuda, orc):
     g = trace(s0, a, step_policy(3000, 40.0, 1e-4))
     K, why, state = _np(g["K"]), _np(g["why"]), _np(g["state"])
     assert np.array_equal(why, o["why"])                  # captured/escaped masks
-    # photon-ring rays amplify rounding-sized differences; the oracle flags
-    # them by its own response to a 1e-12 change of the initial wavevector
+    # rays near the critical curve amplify rounding-sized differences; the
+    # oracle measures each ray's amplification from its own response to a
+    # 1e-12 change of the initial wavevector
+    from test_gpu_vacuum import check_end_states
     op = orc.integrate(orc.perturbed(s0), 3000, 40.0, 1e-4, a)
-    ill = orc.ill_conditioned(o["state"], op["state"]) | (o["K"] != op["K"])
-    assert ill.mean() < 0.05, f"{ill.sum()} ill-conditioned rays"
-    ok = ~ill
-    assert np.array_equal(K[ok], o["K"][ok])
-    assert np.nanmax(rel_err(state[ok], o["state"][ok], floor=1e-3)) < 1e-9
+    check_end_states(orc, K, state, o["K"], o["state"], op["K"], op["state"], "reference rule, 24x24")
 
 
 def test_radius_cal(cuda, orc):

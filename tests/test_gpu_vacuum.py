@@ -4,12 +4,16 @@ policies against the oracle: the reference rule (div 40, tol 1e-4) and the
 fixed-fraction rule (h = 0.05 r clamped to [0.01, 10] M, captured at
 r < 1.01 r_h, escaped at r > 1000 M once r grows).
 
-Bar: captured/escaped masks bit-exact; step counts equal and final x^mu,
-k^mu within 1e-9 relative (floor 1e-3 for components that pass through
-zero) for every well-conditioned ray.  A ray is ill-conditioned when the
-oracle's own end state moves by more than 100x a 1e-12 change of the
-initial wavevector (photon-ring grazers: no FP64 evaluation order
-reproduces them to 1e-9); those are counted, and must stay a few percent.
+Bar: captured/escaped masks bit-exact.  Each ray's amplification A is
+measured on the oracle itself: the relative change of its end state per
+unit relative change of the initial wavevector (1e-12 probe).  Two FP64
+evaluation orders (closed-form Christoffel symbols here, the autodiff
+Jacobian and LU inverse in the reference) differ by ~1e-13 accumulated
+rounding, which reaches the end state multiplied by A.  So: for every ray
+with A <= 1e3 the step count is equal and x^mu, k^mu agree within 1e-9
+relative (floor 1e-3 for components near zero); for every ray with equal
+step count the error stays below max(1e-9, 1e-11 A); the rays with
+A > 1e3 (grazing the critical curve) are counted and printed.
 """
 
 import numpy as np
@@ -20,6 +24,22 @@ from conftest import golden, rel_err
 pytestmark = pytest.mark.gpu
 
 A, INC, RES, NMAX = 0.94, 60.0, 128, 4096
+
+
+def check_end_states(orc, K, st, oK, ost, pK, pst, label):
+    amp = orc.amplification(ost, pst)
+    amp = np.where(oK != pK, np.inf, amp)
+    well = amp <= 1e3
+    assert well.mean() >= 0.85, f"{label}: only {well.mean():.3f} of rays well-conditioned"
+    assert np.array_equal(K[well], oK[well]), f"{label}: step count differs on a well-conditioned ray"
+    err = np.nanmax(rel_err(st, ost, floor=1e-3), axis=1)
+    assert np.nanmax(err[well]) < 1e-9, f"{label}: {np.nanmax(err[well]):.3e}"
+    same = K == oK
+    bound = np.maximum(1e-9, 1e-11 * amp)
+    assert np.all(err[same] <= bound[same]), f"{label}: error above the conditioning bound"
+    print(f"{label}: {len(K)} rays, {int((~well).sum())} with amplification > 1e3, "
+          f"{int((~same).sum())} with a different step count, max error on well-conditioned rays "
+          f"{np.nanmax(err[well]):.2e}")
 
 
 @pytest.fixture(scope="module")
@@ -36,12 +56,7 @@ def test_vacuum_reference_policy(cuda, orc, s0):
     assert np.array_equal(why, o["why"])
     cap = why == 1
     assert 0.05 < cap.mean() < 0.6          # a shadow is there
-    ill = orc.ill_conditioned(o["state"], op["state"]) | (o["K"] != op["K"])
-    print(f"vacuum reference policy: {ill.sum()} of {len(K)} rays ill-conditioned")
-    assert ill.mean() < 0.05
-    ok = ~ill
-    assert np.array_equal(K[ok], o["K"][ok])
-    assert np.nanmax(rel_err(st[ok], o["state"][ok], floor=1e-3)) < 1e-9
+    check_end_states(orc, K, st, o["K"], o["state"], op["K"], op["state"], "vacuum, reference rule")
 
 
 def test_vacuum_fixed_policy(cuda, orc, s0):
@@ -52,12 +67,7 @@ def test_vacuum_fixed_policy(cuda, orc, s0):
     why, K, st = (g[k].cpu().numpy() for k in ("why", "K", "state"))
     assert np.array_equal(why, o["why"])
     assert set(np.unique(why)) <= {1, 2}     # every ray captured or escaped within 4096 steps
-    ill = orc.ill_conditioned(o["state"], op["state"]) | (o["nsteps"] != op["nsteps"])
-    print(f"vacuum fixed policy: {ill.sum()} of {len(K)} rays ill-conditioned")
-    assert ill.mean() < 0.05
-    ok = ~ill
-    assert np.array_equal(K[ok], o["nsteps"][ok])
-    assert np.nanmax(rel_err(st[ok], o["state"][ok], floor=1e-3)) < 1e-9
+    check_end_states(orc, K, st, o["nsteps"], o["state"], op["nsteps"], op["state"], "vacuum, fixed-fraction rule")
 
 
 @pytest.mark.parametrize("key", ["test1", "test2", "test3", "test4"])
