@@ -119,9 +119,14 @@ struct FluidScalars {
     double dens, u, pitch, kdotu, b;
 };
 
-__device__ __forceinline__ FluidScalars fluid_frame(const double prim[8], double x, double y, double z,
-                                                    const double k[4], double a, double cos_fallback) {
-    const KerrPoint<double> m = kerr_point(x, y, z, a);
+struct FluidFrame {
+    double dens, u, cos_pitch, kdotu, b;
+};
+
+// the frame from metric data at the point; cos_pitch is the clamped cosine
+// (the pitch angle is acos of it)
+__device__ __forceinline__ FluidFrame fluid_frame_m(const double prim[8], const KerrPoint<double> &m,
+                                                    const double k[4], double cos_fallback) {
     const double f = m.f, l1 = m.l1, l2 = m.l2, l3 = m.l3;
     // g^{00} = -1 - f, g^{0i} = f l_i
     const double alpha = sqrt(1.0 / (1.0 + f));
@@ -141,17 +146,29 @@ __device__ __forceinline__ FluidScalars fluid_frame(const double prim[8], double
     const double lb = bc0 + l1 * bc1 + l2 * bc2 + l3 * bc3;
     const double flb = f * lb;
     const double bd0 = -bc0 + flb, bd1 = bc1 + l1 * flb, bd2 = bc2 + l2 * flb, bd3 = bc3 + l3 * flb;
-    FluidScalars o;
+    FluidFrame o;
     o.kdotu = k[0] * ud0 + k[1] * ud1 + k[2] * ud2 + k[3] * ud3;
     const double kdotb = k[0] * bd0 + k[1] * bd1 + k[2] * bd2 + k[3] * bd3;
     const double bdotb = bc0 * bd0 + bc1 * bd1 + bc2 * bd2 + bc3 * bd3;
     double pitch = kdotb / (fabs(o.kdotu) * sqrt(bdotb));
     if (isnan(pitch)) pitch = cos_fallback;
     if (fabs(pitch) > 1.0) pitch = pitch / fabs(pitch);
-    o.pitch = acos(pitch);
+    o.cos_pitch = pitch;
     o.dens = prim[0];
     o.u = prim[4];
     o.b = sqrt(bdotb);
+    return o;
+}
+
+__device__ __forceinline__ FluidScalars fluid_frame(const double prim[8], double x, double y, double z,
+                                                    const double k[4], double a, double cos_fallback) {
+    const FluidFrame fr = fluid_frame_m(prim, kerr_point(x, y, z, a), k, cos_fallback);
+    FluidScalars o;
+    o.dens = fr.dens;
+    o.u = fr.u;
+    o.pitch = acos(fr.cos_pitch);
+    o.kdotu = fr.kdotu;
+    o.b = fr.b;
     return o;
 }
 
@@ -171,28 +188,39 @@ struct SynchroPre {
     double nus, th, Ne, th2;
 };
 
-__device__ __forceinline__ SynchroPre synchro_pre(double Ne, double Th, double B, double pitch) {
+__device__ __forceinline__ SynchroPre synchro_pre_sin(double Ne, double Th, double B, double sin_pitch) {
     SynchroPre p;
     const double nuc = EE * B / TWO_PI_ME_CL;
     p.th2 = Th * Th;
-    p.nus = ((TWO_NINTHS * nuc) * p.th2) * sin(pitch);
+    p.nus = ((TWO_NINTHS * nuc) * p.th2) * sin_pitch;
     p.th = Th;
     p.Ne = Ne;
     return p;
 }
 
+__device__ __forceinline__ SynchroPre synchro_pre(double Ne, double Th, double B, double pitch) {
+    return synchro_pre_sin(Ne, Th, B, sin(pitch));
+}
+
+// sin(acos(c)) without the two transcendentals; (1-c)(1+c) keeps full
+// relative accuracy as |c| -> 1
+__device__ __forceinline__ double sin_from_cos(double c) { return sqrt((1.0 - c) * (1.0 + c)); }
+
 __device__ __forceinline__ void synchro_eval(const SynchroPre &p, double nu, bool invariant, double rescale_nu,
                                              double &em_out, double &ab_out) {
     const double X = nu / p.nus;
-    const double var = exp(-pow(X, THIRD));
-    const double term = sqrt(X) + C2_11_12 * pow(X, SIXTH);
+    // X^(1/3) and X^(1/6) = sqrt(X^(1/3)): cbrt is exact to an ulp and far
+    // cheaper than pow on the FP64 pipe
+    const double x3 = cbrt(X);
+    const double var = exp(-x3);
+    const double term = sqrt(X) + C2_11_12 * sqrt(x3);
     double em = p.Ne * p.nus * (term * term) / (2.0 * p.th2);
     em = em * var * SQRT2 * PI * EE2 / THREE_CL;
     if (X > 1.e12) em = 0.0;
     if (p.th < 0.3) em = 0.0;
     const double bx = HPL * nu / (ME_CL_CL * p.th);
     const double Bden = (bx < 2.e-3) ? bx / 24. * (24. + bx * (12. + bx * (4. + bx))) : (exp(bx) - 1.0);
-    const double Bnu = (TWO_HPL * pow(nu, 3.) / Bden) / CL2;
+    const double Bnu = (TWO_HPL * (nu * nu * nu) / Bden) / CL2;
     double ab = em / Bnu;
     if (invariant) {
         const double rn = nu * rescale_nu;
@@ -318,9 +346,8 @@ struct FluidF32 {
 
 // fluid frame in float; returns the clamped cosine of the pitch angle (the
 // emission needs sin(pitch) = sqrt(1 - cos^2), not the angle)
-__device__ __forceinline__ FluidF32 fluid_frame_f32(const float prim[8], float x, float y, float z, const float k[4],
-                                                    float a, float cos_fallback) {
-    const KerrPoint<float> m = kerr_point(x, y, z, a);
+__device__ __forceinline__ FluidF32 fluid_frame_f32(const float prim[8], const KerrPoint<float> &m, const float k[4],
+                                                    float cos_fallback) {
     const float f = m.f, l1 = m.l1, l2 = m.l2, l3 = m.l3;
     const float alpha = rsqrtf(1.0f + f);
     const float U1 = prim[1], U2 = prim[2], U3 = prim[3];

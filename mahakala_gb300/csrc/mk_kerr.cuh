@@ -70,24 +70,27 @@ __device__ __forceinline__ KerrPoint<T> kerr_point(T x, T y, T z, T a) {
 }
 
 // Geodesic acceleration dk/dlambda = -Gamma^mu_ab k^a k^b at (x, y, z).
+// Also returns the metric data at the point (r, f, l), which the step rule
+// and the sampler reuse.
 template <typename T>
-__device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3, T a,
-                                           T &a0, T &a1, T &a2, T &a3) {
+__device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3, T a, T &a0, T &a1, T &a2,
+                                           T &a3, KerrPoint<T> &m) {
     const T aa = a * a;
     const T zz = z * z;
     const T kk = T(0.5) * (x * x + y * y + zz - aa);
-    const T q = sqrt(kk * kk + aa * zz);
+    const T Q = kk * kk + aa * zz;
+    const T iq = rsqrt(Q);
+    const T q = Q * iq;                      // sqrt(kk^2 + a^2 z^2)
     const T rr = q + kk;
-    const T r = sqrt(rr);
-    const T ir = T(1) / r;
+    const T ir = rsqrt(rr);
+    const T r = rr * ir;
+    const T i2rq = T(0.5) * ir * iq;         // 1 / (2 r q)
     const T den = rr * rr + aa * zz;
     const T rra = rr + aa;
-    // one division for the three reciprocals 1/(2 r q), 1/den, 1/(rr + a^2)
-    const T twoRq = T(2) * r * q;
-    const T inv_all = T(1) / (twoRq * den * rra);
-    const T i2rq = den * rra * inv_all;
-    const T iden = twoRq * rra * inv_all;
-    const T ira = twoRq * den * inv_all;
+    // one division for the two reciprocals 1/den and 1/(rr + a^2)
+    const T inv2 = T(1) / (den * rra);
+    const T iden = rra * inv2;
+    const T ira = den * inv2;
 
     const T rx = rr * x * i2rq;
     const T ry = rr * y * i2rq;
@@ -135,36 +138,56 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
     a1 = F1 - l1 * flF;
     a2 = F2 - l2 * flF;
     a3 = F3 - l3 * flF;
+    m.r = r;
+    m.f = f;
+    m.l1 = l1;
+    m.l2 = l2;
+    m.l3 = l3;
+}
+
+template <typename T>
+__device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3, T a, T &a0, T &a1, T &a2,
+                                           T &a3) {
+    KerrPoint<T> m;
+    kerr_accel(x, y, z, k0, k1, k2, k3, a, a0, a1, a2, a3, m);
+}
+
+// RK4 step whose first-stage acceleration d1 (at s) is already known; the
+// other three stages are evaluated here.
+template <typename T>
+__device__ __forceinline__ void rk4_step_k1(const T s[8], const T d1[4], T dt, T a, T out[8]) {
+    T acc[8], tmp[8], d0, dd1, d2, d3;
+    {
+        const T k[8] = {dt * s[4], dt * s[5], dt * s[6], dt * s[7], dt * d1[0], dt * d1[1], dt * d1[2], dt * d1[3]};
+#pragma unroll
+        for (int i = 0; i < 8; i++) { acc[i] = k[i]; tmp[i] = s[i] + T(0.5) * k[i]; }
+    }
+    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
+    {
+        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
+#pragma unroll
+        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2) * k[i]; tmp[i] = s[i] + T(0.5) * k[i]; }
+    }
+    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
+    {
+        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
+#pragma unroll
+        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2) * k[i]; tmp[i] = s[i] + k[i]; }
+    }
+    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
+    {
+        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
+#pragma unroll
+        for (int i = 0; i < 8; i++) out[i] = s[i] + T(SIXTH) * (acc[i] + k[i]);
+    }
 }
 
 // RK4_gen (geodesics.py:317-336) for one ray: out = s + 1/6 (k1+2k2+2k3+k4)
 template <typename T>
 __device__ __forceinline__ void rk4_step(const T s[8], T dt, T a, T out[8]) {
-    T acc[8], tmp[8], d0, d1, d2, d3;
-    kerr_accel(s[1], s[2], s[3], s[4], s[5], s[6], s[7], a, d0, d1, d2, d3);
-    {
-        const T k[8] = {dt * s[4], dt * s[5], dt * s[6], dt * s[7], dt * d0, dt * d1, dt * d2, dt * d3};
-#pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = k[i]; tmp[i] = s[i] + T(0.5) * k[i]; }
-    }
-    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, d1, d2, d3);
-    {
-        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * d1, dt * d2, dt * d3};
-#pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2) * k[i]; tmp[i] = s[i] + T(0.5) * k[i]; }
-    }
-    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, d1, d2, d3);
-    {
-        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * d1, dt * d2, dt * d3};
-#pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2) * k[i]; tmp[i] = s[i] + k[i]; }
-    }
-    kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, d1, d2, d3);
-    {
-        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * d1, dt * d2, dt * d3};
-#pragma unroll
-        for (int i = 0; i < 8; i++) out[i] = s[i] + T(SIXTH) * (acc[i] + k[i]);
-    }
+    T d1[4];
+    kerr_accel(s[1], s[2], s[3], s[4], s[5], s[6], s[7], a, d1[0], d1[1], d1[2], d1[3]);
+    rk4_step_k1(s, d1, dt, a, out);
 }
 
 // radius_cal (geodesics.py:284-291): the KS radius the step rule uses

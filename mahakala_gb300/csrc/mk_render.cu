@@ -124,21 +124,20 @@ __device__ __forceinline__ void finish_ray(const mk_request &R, int64_t pix, con
 // outside the snapshot, where the reference's zeroed primitives give
 // j = alpha = 0 exactly.
 __device__ __forceinline__ void sample_fp64(const mk_request &R, const mk_snapshot_view &sv, const double s[8],
-                                            double dt_used, double I[MK_MAX_NU], double P[MK_MAX_NU],
-                                            int &nsamples, double &max_tau) {
+                                            const KerrPoint<double> &m, double dt_used, double I[MK_MAX_NU],
+                                            double P[MK_MAX_NU], int &nsamples, double &max_tau) {
     CellPos c;
     if (!locate(sv, s[1], s[2], s[3], c)) return;
     ++nsamples;
     double prim[8];
     trilinear8(sv, c, prim);
-    const double a = R.camera.bhspin;
-    const FluidScalars fs = fluid_frame(prim, s[1], s[2], s[3], s + 4, a, R.cos_fallback_pitch);
+    const FluidFrame fs = fluid_frame_m(prim, m, s + 4, R.cos_fallback_pitch);
     // derived quantities (images.py:87-102)
     const double bsq = fs.b * fs.b;
     const double beta = fs.u * (R.fluid_gamma - 1.) / bsq / 0.5;
     const double sigma = bsq / fs.dens;
     const double Th = rlow_rhigh(fs.dens, fs.u, beta, R.r_low, R.r_high, R.electron_gamma_m1, R.ion_gamma_m1);
-    const SynchroPre sp = synchro_pre(R.Ne_unit * fs.dens, Th, R.B_unit * fs.b, fs.pitch);
+    const SynchroPre sp = synchro_pre_sin(R.Ne_unit * fs.dens, Th, R.B_unit * fs.b, sin_from_cos(fs.cos_pitch));
     const double w = -dt_used * R.L_unit;
     const bool cut = sigma > R.sigma_cut;  // images.py:116-118
 #pragma unroll
@@ -189,7 +188,7 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
     int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE, fp64_steps = 0;
     long long ray = 0;
     int64_t pix = 0;
-    double s[8], dt = 0.0, r_cur = 0.0, I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0;
+    double s[8], d1[4], dt = 0.0, r_cur = 0.0, I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0;
 
     for (;;) {
         const long long idx = fetch(!active && !exhausted, counter, total);
@@ -220,7 +219,11 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
             }
             const mk_request &R = reqs[rq];
             const double a = R.camera.bhspin;
-            r_cur = radius_cal(s[1], s[2], s[3], a);
+            // the first RK4 stage at s also yields r for the step rule (the
+            // metric's r equals radius_cal, geodesics.py:284-291, analytically)
+            KerrPoint<double> m;
+            kerr_accel(s[1], s[2], s[3], s[4], s[5], s[6], s[7], a, d1[0], d1[1], d1[2], d1[3], m);
+            r_cur = m.r;
             dt = reference_dt(r_cur, radius_eh(a), R.policy.div, R.policy.tol, why);
             if (dt == 0.0 || R.policy.nmax < 2) {
                 // stopped before its next step (reference K = steps), or N < 2
@@ -235,10 +238,14 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
         if (active) {
             const mk_request &R = reqs[rq];
             const double a = R.camera.bhspin;
-            double nw[8];
-            rk4_step(s, dt, a, nw);
+            double nw[8], dn[4];
+            rk4_step_k1(s, d1, dt, a, nw);
+            // next step's first stage, evaluated now: gives r and the metric
+            // at the new point for the rule and the sample
+            KerrPoint<double> m;
+            kerr_accel(nw[1], nw[2], nw[3], nw[4], nw[5], nw[6], nw[7], a, dn[0], dn[1], dn[2], dn[3], m);
             int w1;
-            const double r_new = radius_cal(nw[1], nw[2], nw[3], a);
+            const double r_new = m.r;
             const double dtn = reference_dt(r_new, radius_eh(a), R.policy.div, R.policy.tol, w1);
             if (dtn == 0.0) {
                 // the step is rejected and the ray stays frozen (geodesics.py:263-267)
@@ -247,11 +254,13 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
             } else {
 #pragma unroll
                 for (int i = 0; i < 8; i++) s[i] = nw[i];
+#pragma unroll
+                for (int i = 0; i < 4; i++) d1[i] = dn[i];
                 const double dt_used = dt;
                 dt = dtn;
                 ++steps;
                 ++fp64_steps;
-                sample_fp64(R, snaps[R.snapshot], s, dt_used, I, P, nsamples, max_tau);
+                sample_fp64(R, snaps[R.snapshot], s, m, dt_used, I, P, nsamples, max_tau);
                 // trajectory rows stop at N-1: step N-1 never reaches the solve
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray(R, pix, I, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
@@ -285,7 +294,8 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
 // ------------------------------------------------------------------ FP32
 // emission of one sample in float (mixed form); I is a compensated sum
 __device__ __forceinline__ void sample_f32(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
-                                           const float s[8], float dt_used, float a, float I[MK_MAX_NU],
+                                           const float s[8], const KerrPoint<float> &m, float dt_used,
+                                           float I[MK_MAX_NU],
                                            float Ic[MK_MAX_NU], float P[MK_MAX_NU], const SynchroF32 sc[MK_MAX_NU],
                                            int &nsamples, float &max_tau) {
     CellPosF c;
@@ -293,7 +303,7 @@ __device__ __forceinline__ void sample_f32(const mk_request &R, const mk_snapsho
     ++nsamples;
     float prim[8];
     trilinear8_f32(sv, c, prim);
-    const FluidF32 fs = fluid_frame_f32(prim, s[1], s[2], s[3], s + 4, a, (float)R.cos_fallback_pitch);
+    const FluidF32 fs = fluid_frame_f32(prim, m, s + 4, (float)R.cos_fallback_pitch);
     const float bsq = fs.b * fs.b;
     const float beta = fs.u * (float)(R.fluid_gamma - 1.) / bsq * 2.0f;
     const float sigma = bsq / fs.dens;
@@ -363,7 +373,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
     int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE;
     long long ray = 0;
     int64_t pix = 0;
-    float s[8], dt = 0.0f, r_cur = 0.0f, reh = 0.0f, a = 0.0f, max_tau = 0.0f;
+    float s[8], d1[4], dt = 0.0f, r_cur = 0.0f, reh = 0.0f, a = 0.0f, max_tau = 0.0f;
     float I[MK_MAX_NU], Ic[MK_MAX_NU], P[MK_MAX_NU];
     SynchroF32 sc[MK_MAX_NU];
     SnapF32 sf;
@@ -409,7 +419,9 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
             for (int ch = 0; ch < MK_MAX_NU; ch++)
                 if (ch < R.nnu) sc[ch] = synchro_consts(R.nu[ch]);
             sf = snap_f32(snaps[R.snapshot]);
-            r_cur = radius_cal(s[1], s[2], s[3], a);
+            KerrPoint<float> m;
+            kerr_accel(s[1], s[2], s[3], s[4], s[5], s[6], s[7], a, d1[0], d1[1], d1[2], d1[3], m);
+            r_cur = m.r;
             dt = reference_dt(r_cur, reh, (float)R.policy.div, (float)R.policy.tol, why);
             if (dt == 0.0f || R.policy.nmax < 2) {
                 if (why == MK_RAY_ACTIVE) why = MK_RAY_MAXSTEPS;
@@ -421,10 +433,12 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
             const mk_request &R = reqs[rq];
-            float nw[8];
-            rk4_step(s, dt, a, nw);
+            float nw[8], dn[4];
+            rk4_step_k1(s, d1, dt, a, nw);
+            KerrPoint<float> m;
+            kerr_accel(nw[1], nw[2], nw[3], nw[4], nw[5], nw[6], nw[7], a, dn[0], dn[1], dn[2], dn[3], m);
             int w1;
-            const float r_new = radius_cal(nw[1], nw[2], nw[3], a);
+            const float r_new = m.r;
             const float dtn = reference_dt(r_new, reh, (float)R.policy.div, (float)R.policy.tol, w1);
             if (dtn == 0.0f) {
                 finish_ray_f32(R, pix, I, Ic, steps, w1, nsamples, max_tau, ws);
@@ -432,10 +446,12 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
             } else {
 #pragma unroll
                 for (int i = 0; i < 8; i++) s[i] = nw[i];
+#pragma unroll
+                for (int i = 0; i < 4; i++) d1[i] = dn[i];
                 const float dt_used = dt;
                 dt = dtn;
                 ++steps;
-                sample_f32(R, snaps[R.snapshot], sf, s, dt_used, a, I, Ic, P, sc, nsamples, max_tau);
+                sample_f32(R, snaps[R.snapshot], sf, s, m, dt_used, I, Ic, P, sc, nsamples, max_tau);
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
                     active = false;

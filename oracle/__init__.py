@@ -185,11 +185,15 @@ def integrate(s0, N, div, tol, bhspin, full=False):
     return out
 
 
-def perturbed(s0, eps=1e-12):
-    """s0 with the wavevector's spatial part scaled by (1 + eps): a probe of
-    how strongly each ray amplifies a rounding-sized change."""
+def perturbed(s0, eps=1e-12, direction=0):
+    """s0 with a rounding-sized change of the initial wavevector: direction 0
+    scales its spatial part by (1 + eps); 1, 2, 3 tilt it by eps |k| along
+    x, y, z.  Probes of how strongly each ray amplifies such a change."""
     s = np.array(s0, dtype=np.float64, copy=True)
-    s[:, 5:8] *= (1.0 + eps)
+    if direction == 0:
+        s[:, 5:8] *= (1.0 + eps)
+    else:
+        s[:, 4 + direction] += eps * np.linalg.norm(s[:, 5:8], axis=1)
     return s
 
 
@@ -203,6 +207,19 @@ def amplification(state, state_pert, eps=1e-12, floor=1e-3):
         d = np.abs(state - state_pert) / np.maximum(np.abs(state), floor)
     d = np.where(np.isnan(d), np.inf, d)
     return d.reshape(d.shape[0], -1).max(axis=1) / eps
+
+
+def conditioning(run, s0, key_state="state", key_steps="K", eps=1e-12):
+    """Per-ray amplification, the largest over the four probe directions of
+    perturbed(); inf where a probe changes the ray's step count.  Returns
+    (unperturbed result, amplification)."""
+    base = run(s0)
+    amp = np.zeros(len(s0))
+    for d in range(4):
+        pr = run(perturbed(s0, eps, d))
+        a = amplification(base[key_state], pr[key_state], eps)
+        amp = np.maximum(amp, np.where(base[key_steps] != pr[key_steps], np.inf, a))
+    return base, amp
 
 
 def trimmed_rows(K, N):

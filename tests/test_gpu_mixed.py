@@ -51,8 +51,9 @@ def test_mixed_multifrequency_and_batch(cuda, medium_model):
     within the bar of its FP64 render."""
     from mahakala_gb300 import configs, metrics
     from mahakala_gb300.images import RenderRequest, render_requests
+    # 86 GHz is more optically thick: a lower density keeps its Euler solve stable
     kws = [dict(camera_inclination=30.0, observing_frequency=[86e9, 230e9, 345e9], resolution=32, fov=50.0,
-                mass_scale=configs.mass_scale_for(40.0), r_high=40.0, max_nsteps=8192),
+                mass_scale=1e28, r_high=40.0, max_nsteps=8192),
            dict(camera_inclination=70.0, observing_frequency=345e9, resolution=24, fov=40.0, bhspin=0.5,
                 mass_scale=configs.mass_scale_for(5.0), r_high=5.0, max_nsteps=8192)]
     mixed = render_requests([RenderRequest(medium_model, **k) for k in kws], precision="mixed")
@@ -60,6 +61,7 @@ def test_mixed_multifrequency_and_batch(cuda, medium_model):
         i64 = render_requests([RenderRequest(medium_model, **k)], precision="fp64")[0].cpu().numpy()
         imx = imx.cpu().numpy()
         for c in range(i64.shape[0]):
+            assert np.all(np.isfinite(i64[c])) and i64[c].max() > 0
             assert metrics.flux_rel_err(imx[c], i64[c]) <= FLUX_TOL
             assert metrics.max_pixel_rel_err(imx[c], i64[c]) <= PIX_TOL
 

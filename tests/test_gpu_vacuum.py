@@ -5,15 +5,17 @@ fixed-fraction rule (h = 0.05 r clamped to [0.01, 10] M, captured at
 r < 1.01 r_h, escaped at r > 1000 M once r grows).
 
 Bar: captured/escaped masks bit-exact.  Each ray's amplification A is
-measured on the oracle itself: the relative change of its end state per
-unit relative change of the initial wavevector (1e-12 probe).  Two FP64
+measured on the oracle itself: the largest relative change of its end
+state per unit relative change of the initial wavevector over four probe
+directions (scale, and tilts along x, y, z, each 1e-12).  Two FP64
 evaluation orders (closed-form Christoffel symbols here, the autodiff
-Jacobian and LU inverse in the reference) differ by ~1e-13 accumulated
-rounding, which reaches the end state multiplied by A.  So: for every ray
-with A <= 1e3 the step count is equal and x^mu, k^mu agree within 1e-9
-relative (floor 1e-3 for components near zero); for every ray with equal
-step count the error stays below max(1e-9, 1e-11 A); the rays with
-A > 1e3 (grazing the critical curve) are counted and printed.
+Jacobian and LU inverse in the reference) differ by ~1e-13 of accumulated
+rounding, which reaches the end state multiplied by A -- and A exceeds 1e3
+for about half the rays of this camera (lensing near the shadow, blueshift
+near the horizon).  So: step counts equal on at least 99 % of rays; on
+every ray with equal step count the end-state error (relative, floor 1e-3)
+stays under max(1e-9, 1e-12 A); at least 90 % of all rays are within
+1e-9; the counts are printed.
 """
 
 import numpy as np
@@ -26,20 +28,18 @@ pytestmark = pytest.mark.gpu
 A, INC, RES, NMAX = 0.94, 60.0, 128, 4096
 
 
-def check_end_states(orc, K, st, oK, ost, pK, pst, label):
-    amp = orc.amplification(ost, pst)
-    amp = np.where(oK != pK, np.inf, amp)
-    well = amp <= 1e3
-    assert well.mean() >= 0.85, f"{label}: only {well.mean():.3f} of rays well-conditioned"
-    assert np.array_equal(K[well], oK[well]), f"{label}: step count differs on a well-conditioned ray"
+def check_end_states(orc, K, st, oK, ost, amp, label):
     err = np.nanmax(rel_err(st, ost, floor=1e-3), axis=1)
-    assert np.nanmax(err[well]) < 1e-9, f"{label}: {np.nanmax(err[well]):.3e}"
     same = K == oK
-    bound = np.maximum(1e-9, 1e-11 * amp)
-    assert np.all(err[same] <= bound[same]), f"{label}: error above the conditioning bound"
-    print(f"{label}: {len(K)} rays, {int((~well).sum())} with amplification > 1e3, "
-          f"{int((~same).sum())} with a different step count, max error on well-conditioned rays "
-          f"{np.nanmax(err[well]):.2e}")
+    assert same.mean() >= 0.99, f"{label}: {int((~same).sum())} rays changed step count"
+    bound = np.maximum(1e-9, 1e-12 * amp)
+    bad = same & ~(err <= bound)
+    assert not bad.any(), f"{label}: {int(bad.sum())} rays above the conditioning bound, worst err {err[bad].max():.2e}"
+    within = same & (err <= 1e-9)
+    assert within.mean() >= 0.90, f"{label}: only {within.mean():.3f} of rays within 1e-9"
+    print(f"{label}: {len(K)} rays; {within.mean() * 100:.2f} % within 1e-9; {int((amp > 1e3).sum())} with "
+          f"amplification > 1e3; {int((~same).sum())} with a different step count; worst error "
+          f"{np.nanmax(err[same]):.2e}")
 
 
 @pytest.fixture(scope="module")
@@ -49,25 +49,23 @@ def s0(orc):
 
 def test_vacuum_reference_policy(cuda, orc, s0):
     from mahakala_gb300.geodesics import step_policy, trace
-    o = orc.integrate(s0, NMAX, 40.0, 1e-4, A)
-    op = orc.integrate(orc.perturbed(s0), NMAX, 40.0, 1e-4, A)
+    o, amp = orc.conditioning(lambda s: orc.integrate(s, NMAX, 40.0, 1e-4, A), s0)
     g = trace(s0, A, step_policy(NMAX, 40.0, 1e-4))
     why, K, st = (g[k].cpu().numpy() for k in ("why", "K", "state"))
     assert np.array_equal(why, o["why"])
     cap = why == 1
     assert 0.05 < cap.mean() < 0.6          # a shadow is there
-    check_end_states(orc, K, st, o["K"], o["state"], op["K"], op["state"], "vacuum, reference rule")
+    check_end_states(orc, K, st, o["K"], o["state"], amp, "vacuum, reference rule")
 
 
 def test_vacuum_fixed_policy(cuda, orc, s0):
     from mahakala_gb300.geodesics import step_policy, trace
-    o = orc.trace_fixed(s0, NMAX, A)
-    op = orc.trace_fixed(orc.perturbed(s0), NMAX, A)
+    o, amp = orc.conditioning(lambda s: orc.trace_fixed(s, NMAX, A), s0, key_steps="nsteps")
     g = trace(s0, A, step_policy(NMAX, kind="fixed"))
     why, K, st = (g[k].cpu().numpy() for k in ("why", "K", "state"))
     assert np.array_equal(why, o["why"])
     assert set(np.unique(why)) <= {1, 2}     # every ray captured or escaped within 4096 steps
-    check_end_states(orc, K, st, o["nsteps"], o["state"], op["nsteps"], op["state"], "vacuum, fixed-fraction rule")
+    check_end_states(orc, K, st, o["nsteps"], o["state"], amp, "vacuum, fixed-fraction rule")
 
 
 @pytest.mark.parametrize("key", ["test1", "test2", "test3", "test4"])
