@@ -190,6 +190,82 @@ __device__ __forceinline__ void rk4_step(const T s[8], T dt, T a, T out[8]) {
     rk4_step_k1(s, d1, dt, a, out);
 }
 
+// ------------------------------------------------------------------------
+// Float pairs (hi + lo) for the mixed form's ray state.  TwoSum is Knuth's
+// error-free addition (TAOCP vol. 2, 4.2.2), FastTwoSum Dekker's (1971)
+// variant for |a| >= |b|; the product error comes from one fused
+// multiply-add.  No step here may be reassociated or contracted (nvcc does
+// neither without fast-math; the products are explicit fmaf).
+struct f2 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ f2 two_sum(float a, float b) {
+    const float s = a + b;
+    const float v = s - a;
+    return {s, (a - (s - v)) + (b - v)};
+}
+
+__device__ __forceinline__ f2 fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ f2 f2_add(f2 x, float y) {
+    f2 s = two_sum(x.hi, y);
+    s.lo += x.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+
+__device__ __forceinline__ f2 f2_add(f2 x, f2 y) {
+    f2 s = two_sum(x.hi, y.hi);
+    s.lo += x.lo + y.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+
+__device__ __forceinline__ f2 f2_mul(f2 x, float b) {
+    const float p = x.hi * b;
+    float e = fmaf(x.hi, b, -p);
+    e = fmaf(x.lo, b, e);
+    return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ f2 f2_from(double d) {
+    const float hi = (float)d;
+    return {hi, (float)(d - (double)hi)};
+}
+
+__device__ __forceinline__ double f2_to(f2 x) { return (double)x.hi + (double)x.lo; }
+
+// RK4 on a float-pair state (X = x^mu, K = k^mu), accelerations in float.
+// The position increment of RK4 is dt k + dt^2/6 (a1 + a2 + a3); its
+// leading term is formed in pair precision, so neither rounding of the
+// position (ulp(1000) = 6e-5 in float) nor of the direction accumulates
+// along the 1000 M approach from the camera.  a1 = acceleration at X, K.
+__device__ __forceinline__ void rk4_step_pair(const f2 X[4], const f2 K[4], const float a1[4], float dt, float a,
+                                              f2 Xo[4], f2 Ko[4]) {
+    float x[4], k[4], t[8], a2[4], a3[4], a4[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) { x[i] = X[i].hi; k[i] = K[i].hi; }
+    const float h = 0.5f * dt;
+#pragma unroll
+    for (int i = 0; i < 4; i++) { t[i] = x[i] + h * k[i]; t[4 + i] = k[i] + h * a1[i]; }
+    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a2[0], a2[1], a2[2], a2[3]);
+#pragma unroll
+    for (int i = 0; i < 4; i++) { t[i] = x[i] + h * (k[i] + h * a1[i]); t[4 + i] = k[i] + h * a2[i]; }
+    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a3[0], a3[1], a3[2], a3[3]);
+#pragma unroll
+    for (int i = 0; i < 4; i++) { t[i] = x[i] + dt * (k[i] + h * a2[i]); t[4 + i] = k[i] + dt * a3[i]; }
+    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a4[0], a4[1], a4[2], a4[3]);
+    const float c = dt * dt * (1.0f / 6.0f);
+    const float d = dt * (1.0f / 6.0f);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        Xo[i] = f2_add(X[i], f2_add(f2_mul(K[i], dt), c * (a1[i] + a2[i] + a3[i])));
+        Ko[i] = f2_add(K[i], d * (a1[i] + 2.0f * a2[i] + 2.0f * a3[i] + a4[i]));
+    }
+}
+
 // radius_cal (geodesics.py:284-291): the KS radius the step rule uses
 template <typename T>
 __device__ __forceinline__ T radius_cal(T x, T y, T z, T a) {

@@ -361,6 +361,8 @@ __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix,
 
 // FP32 render phase.  SRC_CAMERA: mixed-form phase A from the camera, with
 // hand-off to the FP64 queue.  SRC_QUEUE: phase C over the FP32 queue.
+// The ray state is a float pair per component (rk4_step_pair); the
+// accelerations, the sampling and the emission are plain float.
 template <int SRC>
 __global__ void __launch_bounds__(RENDER_THREADS)
 render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
@@ -373,7 +375,8 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
     int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE;
     long long ray = 0;
     int64_t pix = 0;
-    float s[8], d1[4], dt = 0.0f, r_cur = 0.0f, reh = 0.0f, a = 0.0f, max_tau = 0.0f;
+    f2 X[4], K[4];
+    float d1[4], dt = 0.0f, r_cur = 0.0f, reh = 0.0f, a = 0.0f, max_tau = 0.0f;
     float I[MK_MAX_NU], Ic[MK_MAX_NU], P[MK_MAX_NU];
     SynchroF32 sc[MK_MAX_NU];
     SnapF32 sf;
@@ -412,7 +415,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
             }
             const mk_request &R = reqs[rq];
 #pragma unroll
-            for (int i = 0; i < 8; i++) s[i] = (float)s64[i];
+            for (int i = 0; i < 4; i++) { X[i] = f2_from(s64[i]); K[i] = f2_from(s64[4 + i]); }
             a = (float)R.camera.bhspin;
             reh = (float)radius_eh(R.camera.bhspin);
 #pragma unroll
@@ -420,7 +423,8 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 if (ch < R.nnu) sc[ch] = synchro_consts(R.nu[ch]);
             sf = snap_f32(snaps[R.snapshot]);
             KerrPoint<float> m;
-            kerr_accel(s[1], s[2], s[3], s[4], s[5], s[6], s[7], a, d1[0], d1[1], d1[2], d1[3], m);
+            kerr_accel(X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi, a, d1[0], d1[1], d1[2], d1[3],
+                       m);
             r_cur = m.r;
             dt = reference_dt(r_cur, reh, (float)R.policy.div, (float)R.policy.tol, why);
             if (dt == 0.0f || R.policy.nmax < 2) {
@@ -433,10 +437,12 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
             const mk_request &R = reqs[rq];
-            float nw[8], dn[4];
-            rk4_step_k1(s, d1, dt, a, nw);
+            f2 Xn[4], Kn[4];
+            float dn[4];
+            rk4_step_pair(X, K, d1, dt, a, Xn, Kn);
             KerrPoint<float> m;
-            kerr_accel(nw[1], nw[2], nw[3], nw[4], nw[5], nw[6], nw[7], a, dn[0], dn[1], dn[2], dn[3], m);
+            kerr_accel(Xn[1].hi, Xn[2].hi, Xn[3].hi, Kn[0].hi, Kn[1].hi, Kn[2].hi, Kn[3].hi, a, dn[0], dn[1], dn[2],
+                       dn[3], m);
             int w1;
             const float r_new = m.r;
             const float dtn = reference_dt(r_new, reh, (float)R.policy.div, (float)R.policy.tol, w1);
@@ -445,13 +451,12 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 active = false;
             } else {
 #pragma unroll
-                for (int i = 0; i < 8; i++) s[i] = nw[i];
-#pragma unroll
-                for (int i = 0; i < 4; i++) d1[i] = dn[i];
+                for (int i = 0; i < 4; i++) { X[i] = Xn[i]; K[i] = Kn[i]; d1[i] = dn[i]; }
                 const float dt_used = dt;
                 dt = dtn;
                 ++steps;
-                sample_f32(R, snaps[R.snapshot], sf, s, m, dt_used, I, Ic, P, sc, nsamples, max_tau);
+                const float sh[8] = {X[0].hi, X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi};
+                sample_f32(R, snaps[R.snapshot], sf, sh, m, dt_used, I, Ic, P, sc, nsamples, max_tau);
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
                     active = false;
@@ -462,7 +467,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                     if ((long long)slot < capacity) {
                         RayRecord &q = q64[slot];
 #pragma unroll
-                        for (int i = 0; i < 8; i++) q.s[i] = (double)s[i];
+                        for (int i = 0; i < 4; i++) { q.s[i] = f2_to(X[i]); q.s[4 + i] = f2_to(K[i]); }
 #pragma unroll
                         for (int ch = 0; ch < MK_MAX_NU; ch++) {
                             q.I[ch] = (double)I[ch] - (double)Ic[ch];
@@ -543,10 +548,15 @@ extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
         <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA>, 1), total_rays), RENDER_THREADS, 0, st>>>(
             reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap);
     MK_LAUNCHED("render_f32_kernel (camera)");
-    // the queues' sizes are only known on the device: full persistent grids
-    render_fp64_kernel<SRC_QUEUE>
-        <<<persistent_grid(blocks_per_sm(render_fp64_kernel<SRC_QUEUE>, 2), total_rays), RENDER_THREADS, 0, st>>>(
-            reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
+    // The queues' sizes are only known on the device: persistent grids.
+    // Phase B runs one warp per block, 4 blocks per SM: the few FP64 rays
+    // spread over every SM sub-partition instead of queuing on the FP64
+    // units of a few SMs (one FP64 warp instruction occupies a
+    // sub-partition's FP64 unit for tens of cycles on this part).
+    {
+        unsigned grid = (unsigned)device_sm_count() * 4;
+        render_fp64_kernel<SRC_QUEUE><<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
+    }
     MK_LAUNCHED("render_fp64_kernel (queue)");
     render_f32_kernel<SRC_QUEUE>
         <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE>, 3), total_rays), RENDER_THREADS, 0, st>>>(
