@@ -50,8 +50,9 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"],
-                   help="both: time FP64 and mixed, headline the mixed form and report its error vs FP64")
+    p.add_argument("--precision", default="all", choices=["fp64", "mixed", "mixed_df", "all"],
+                   help="all: time FP64, mixed and mixed_df, headline the mixed form and report each mixed "
+                        "form's error vs FP64")
     p.add_argument("--workload", default="render256", choices=["render256", "stress1024"])
     p.add_argument("--cpu-sample-rays", type=int, default=0, help="rays per CPU baseline sample (0 = auto)")
     p.add_argument("--resolution", type=int, default=0, help="override the image size (profiling small cases)")
@@ -247,8 +248,8 @@ def main():
     from mahakala_gb300.grmhd.athenak import AthenakFluidModel
     from mahakala_gb300.images import PreparedRender, image_flux_jy, make_image
 
-    forms = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
-    head = forms[-1]
+    forms = ["fp64", "mixed", "mixed_df"] if args.precision == "all" else [args.precision]
+    head = "mixed" if "mixed" in forms else forms[0]
     spec, desc = workload(args.workload, args.resolution, head)
     t_gen = time.perf_counter()
     arrays = spec.snapshot.build()
@@ -341,7 +342,7 @@ def main():
     line = {
         "metric": "rays/s", "value": world * rays / t_head, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_head, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32+f64",
+        "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f32+f64", "mixed_df": "f32+f32x2"}[head],
         "data": "synthetic (seeded snapshot, no external data)",
         "config": {"workload": desc, "precision": head,
                    "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write, untimed)",
@@ -351,16 +352,18 @@ def main():
     }
     for form in forms:
         line[form] = form_line(form)
-    if "fp64" in res and "mixed" in res:
-        a, b = res["mixed"], res["fp64"]
+    for form in ("mixed", "mixed_df"):
+        if "fp64" not in res or form not in res:
+            continue
+        a, b = res[form], res["fp64"]
         errs = [metrics.compare(a["image"][c], b["image"][c], a["status"], b["status"], spec.fov)
                 for c in range(nnu)]
-        line["mixed_vs_fp64"] = {"speedup": b["t_step"] / a["t_step"],
-                                 "flux_rel_err": max(e["flux_rel_err"] for e in errs),
-                                 "max_pixel_rel_err": max(e["max_pixel_rel_err"] for e in errs),
-                                 "shadow_diameter": errs[0]["shadow_diameter"],
-                                 "shadow_diameter_fp64": errs[0]["shadow_diameter_fp64"],
-                                 "pixel_floor": "max(|I_fp64|, 1e-4 max I_fp64)"}
+        line[form + "_vs_fp64"] = {"speedup": b["t_step"] / a["t_step"],
+                                   "flux_rel_err": max(e["flux_rel_err"] for e in errs),
+                                   "max_pixel_rel_err": max(e["max_pixel_rel_err"] for e in errs),
+                                   "shadow_diameter": errs[0]["shadow_diameter"],
+                                   "shadow_diameter_fp64": errs[0]["shadow_diameter_fp64"],
+                                   "pixel_floor": "max(|I_fp64|, 1e-4 max I_fp64)"}
     line.update({
         "roofline": roofline(head),
         "cpu_baseline": {"value": cpu_val, "unit": "rays/s", "cores": threads, "kind": "port",

@@ -44,7 +44,12 @@ typedef enum {
     MK_RAY_NAN = 4
 } mk_ray_status;
 
-typedef enum { MK_FP64 = 0, MK_MIXED = 1 } mk_precision;
+/* MK_FP64: every operation in binary64.  MK_MIXED: FP32 with binary64 near
+   the hole and at photon-ring turning points.  MK_MIXED_DF: as MK_MIXED but
+   the near-hole geodesic runs in double-float (pairs of FP32, ~1e-13
+   relative) instead of binary64 -- not IEEE FP64, faster on parts whose
+   FP64 rate is a small fraction of FP32. */
+typedef enum { MK_FP64 = 0, MK_MIXED = 1, MK_MIXED_DF = 2 } mk_precision;
 
 typedef enum {
     /* dt = -(r - r_EH)/div, stop (and reject the step) when the next dt

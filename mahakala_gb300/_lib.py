@@ -18,7 +18,7 @@ _SZ = _c.c_size_t
 
 MK_OK, MK_ERR_ARG, MK_ERR_CUDA, MK_ERR_LIMIT, MK_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
 MK_RAY_ACTIVE, MK_RAY_CAPTURED, MK_RAY_ESCAPED, MK_RAY_MAXSTEPS, MK_RAY_NAN = 0, 1, 2, 3, 4
-MK_FP64, MK_MIXED = 0, 1
+MK_FP64, MK_MIXED, MK_MIXED_DF = 0, 1, 2
 MK_POLICY_REFERENCE, MK_POLICY_FIXED = 0, 1
 MK_CAMERA_GRID, MK_CAMERA_EQUATOR = 0, 1
 MK_MAX_NU = 4

@@ -22,6 +22,7 @@
 #include <stdint.h>
 
 #include "mahakala_gb300.h"
+#include "mk_dd.cuh"
 
 namespace mk {
 
@@ -79,10 +80,10 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
     const T zz = z * z;
     const T kk = T(0.5) * (x * x + y * y + zz - aa);
     const T Q = kk * kk + aa * zz;
-    const T iq = rsqrt(Q);
+    const T iq = inv_sqrt(Q);
     const T q = Q * iq;                      // sqrt(kk^2 + a^2 z^2)
     const T rr = q + kk;
-    const T ir = rsqrt(rr);
+    const T ir = inv_sqrt(rr);
     const T r = rr * ir;
     const T i2rq = T(0.5) * ir * iq;         // 1 / (2 r q)
     const T den = rr * rr + aa * zz;

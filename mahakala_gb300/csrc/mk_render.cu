@@ -33,6 +33,7 @@
 //   intensity accumulates with a compensated (Kahan) FP32 sum and the
 //   transmission product in FP32; both move to FP64 with the ray.
 #include "mk_common.cuh"
+#include "mk_dd.cuh"
 #include "mk_fluid.cuh"
 
 namespace mk {
@@ -171,12 +172,120 @@ __device__ __forceinline__ void renull_fp64(double s[8], double a) {
     s[4] = fabs(r1 - s[4]) < fabs(r2 - s[4]) ? r1 : r2;
 }
 
+// ------------------------------------------------------------------ FP32
+// emission coefficients of one sample in float (mixed form): em, ab per
+// frequency (invariant, rescaled as in the FP64 path), and the step weight
+// w = -dt L.  Returns false outside the snapshot (no contribution).
+__device__ __forceinline__ bool emission_f32(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
+                                             const float s[8], const KerrPoint<float> &m,
+                                             const SynchroF32 sc[MK_MAX_NU], float em_out[MK_MAX_NU],
+                                             float ab_out[MK_MAX_NU]) {
+    CellPosF c;
+    if (!locate_f32(sv, sf, s[1], s[2], s[3], c)) return false;
+    float prim[8];
+    trilinear8_f32(sv, c, prim);
+    const FluidF32 fs = fluid_frame_f32(prim, m, s + 4, (float)R.cos_fallback_pitch);
+    const float bsq = fs.b * fs.b;
+    const float beta = fs.u * (float)(R.fluid_gamma - 1.) / bsq * 2.0f;
+    const float sigma = bsq / fs.dens;
+    const float b2 = beta * beta;
+    const float T_ratio = ((float)R.r_high * b2 + (float)R.r_low) / (1.0f + b2);
+    const float gem1 = (float)R.electron_gamma_m1, gim1 = (float)R.ion_gamma_m1;
+    // Theta_e = (MP/ME) u gem1 gim1 / (dens (gim1 + gem1 T_ratio))
+    const float Th = (float)(MP / ME) * fs.u * gem1 * gim1 / (fs.dens * (gim1 + gem1 * T_ratio));
+    const float Ne = (float)R.Ne_unit * fs.dens;
+    const float Bg = (float)R.B_unit * fs.b;
+    const float sin_p = sqrtf((1.0f - fs.cos_pitch) * (1.0f + fs.cos_pitch));
+    const float th2 = Th * Th;
+    // nus in Hz; nu' = -k.u (observed frequency rescaled to 1)
+    const float nus = (float)(TWO_NINTHS * EE / TWO_PI_ME_CL) * Bg * th2 * sin_p;
+    const float nup = -fs.kdotu;
+    const bool cut = sigma > (float)R.sigma_cut || Th < 0.3f;
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++) {
+        if (ch < R.nnu) {
+            const float nusp = nus * sc[ch].inv_nu;  // nus / nu_obs
+            const float X = nup / nusp;
+            const float x3 = cbrtf(X);
+            const float term = sqrtf(X) + (float)C2_11_12 * sqrtf(x3);
+            // emissivity / nu'^2 (invariant, rescaled): k_em folds
+            // sqrt2 pi EE^2 / (3 CL) and nu_obs
+            float em = Ne * sc[ch].k_em * nusp * term * term / (2.0f * th2) * __expf(-x3) / (nup * nup);
+            if (X > 1.e12f || cut) em = 0.0f;
+            const float bx = sc[ch].k_bx * nup / Th;
+            const float bden = bx < 2.e-3f ? bx / 24.f * (24.f + bx * (12.f + bx * (4.f + bx))) : expm1f(bx);
+            // alpha nu' = (em nu'^2) / B_nu * nu' with B_nu = k_bnu nu'^3 / bden
+            float ab = em * bden / sc[ch].k_bnu;
+            em_out[ch] = isnan(em) ? 0.0f : em;
+            ab_out[ch] = isnan(ab) ? 0.0f : ab;
+        }
+    }
+    return true;
+}
+
+// one FP32 sample folded into a compensated (Kahan) float intensity sum
+__device__ __forceinline__ void sample_f32(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
+                                           const float s[8], const KerrPoint<float> &m, float dt_used,
+                                           float I[MK_MAX_NU], float Ic[MK_MAX_NU], float P[MK_MAX_NU],
+                                           const SynchroF32 sc[MK_MAX_NU], int &nsamples, float &max_tau) {
+    float em[MK_MAX_NU], ab[MK_MAX_NU];
+    if (!emission_f32(R, sv, sf, s, m, sc, em, ab)) return;
+    ++nsamples;
+    const float w = -dt_used * (float)R.L_unit;
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++) {
+        if (ch < R.nnu) {
+            const float tau = w * ab[ch];
+            const float y = (w * em[ch]) * P[ch] - Ic[ch];
+            const float t = I[ch] + y;
+            Ic[ch] = (t - I[ch]) - y;
+            I[ch] = t;
+            P[ch] *= (1.0f - tau);
+            max_tau = fmaxf(max_tau, tau);
+        }
+    }
+}
+
+// FP32 emission at an FP64 or double-float state (mixed-form phase B),
+// accumulated in FP64
+template <typename T>
+__device__ __forceinline__ void sample_f32_at(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
+                                              const T s[8], const KerrPoint<T> &m64, double dt_used,
+                                              double I[MK_MAX_NU], double P[MK_MAX_NU],
+                                              const SynchroF32 sc[MK_MAX_NU], int &nsamples, double &max_tau) {
+    float sf8[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) sf8[i] = to_float(s[i]);
+    KerrPoint<float> m;
+    m.r = to_float(m64.r);
+    m.f = to_float(m64.f);
+    m.l1 = to_float(m64.l1);
+    m.l2 = to_float(m64.l2);
+    m.l3 = to_float(m64.l3);
+    float em[MK_MAX_NU], ab[MK_MAX_NU];
+    if (!emission_f32(R, sv, sf, sf8, m, sc, em, ab)) return;
+    ++nsamples;
+    const double w = -dt_used * R.L_unit;
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++) {
+        if (ch < R.nnu) {
+            const double tau = w * (double)ab[ch];
+            I[ch] += (w * (double)em[ch]) * P[ch];
+            P[ch] *= (1.0 - tau);
+            max_tau = fmax(max_tau, tau);
+        }
+    }
+}
+
 enum { SRC_CAMERA = 0, SRC_QUEUE = 1 };
+
+
 
 // FP64 render.  SRC_CAMERA: every ray of the job, start to end (MK_FP64).
 // SRC_QUEUE: mixed-form phase B over the FP64 queue; rays leaving R_TURN
-// outward go to the FP32 queue.
-template <int SRC>
+// outward go to the FP32 queue.  T is the geodesic arithmetic: double, or
+// dd (double-float pairs) for the MK_MIXED_DF variant of phase B.
+template <int SRC, typename T = double>
 __global__ void __launch_bounds__(RENDER_THREADS)
 render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
                    const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64,
@@ -188,7 +297,10 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
     int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE, fp64_steps = 0;
     long long ray = 0;
     int64_t pix = 0;
-    double s[8], d1[4], dt = 0.0, r_cur = 0.0, I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0;
+    T s[8], d1[4], dt = T(0.0);
+    double r_cur = 0.0, I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0;
+    SynchroF32 sc[MK_MAX_NU];
+    SnapF32 sf;
 
     for (;;) {
         const long long idx = fetch(!active && !exhausted, counter, total);
@@ -198,15 +310,19 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
                 ray = idx;
                 rq = find_request(reqs, nreq, ray);
                 pix = ray - reqs[rq].ray_offset;
-                camera_ray(reqs[rq].camera, pix, s);
+                double s64[8];
+                camera_ray(reqs[rq].camera, pix, s64);
+#pragma unroll
+                for (int i = 0; i < 8; i++) s[i] = T(s64[i]);
                 steps = nsamples = 0;
                 max_tau = 0.0;
 #pragma unroll
                 for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = 0.0; P[ch] = 1.0; }
             } else {
                 const RayRecord &q = q64[idx];
+                double s64[8];
 #pragma unroll
-                for (int i = 0; i < 8; i++) s[i] = q.s[i];
+                for (int i = 0; i < 8; i++) s64[i] = q.s[i];
 #pragma unroll
                 for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = q.I[ch]; P[ch] = q.P[ch]; }
                 max_tau = q.max_tau;
@@ -215,17 +331,25 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
                 nsamples = q.nsamples;
                 rq = q.rq;
                 pix = ray - reqs[rq].ray_offset;
-                renull_fp64(s, reqs[rq].camera.bhspin);
+                renull_fp64(s64, reqs[rq].camera.bhspin);
+#pragma unroll
+                for (int i = 0; i < 8; i++) s[i] = T(s64[i]);
+                const mk_request &Rq = reqs[rq];
+#pragma unroll
+                for (int ch = 0; ch < MK_MAX_NU; ch++)
+                    if (ch < Rq.nnu) sc[ch] = synchro_consts(Rq.nu[ch]);
+                sf = snap_f32(snaps[Rq.snapshot]);
             }
             const mk_request &R = reqs[rq];
-            const double a = R.camera.bhspin;
+            const T a = T(R.camera.bhspin);
             // the first RK4 stage at s also yields r for the step rule (the
             // metric's r equals radius_cal, geodesics.py:284-291, analytically)
-            KerrPoint<double> m;
+            KerrPoint<T> m;
             kerr_accel(s[1], s[2], s[3], s[4], s[5], s[6], s[7], a, d1[0], d1[1], d1[2], d1[3], m);
-            r_cur = m.r;
-            dt = reference_dt(r_cur, radius_eh(a), R.policy.div, R.policy.tol, why);
-            if (dt == 0.0 || R.policy.nmax < 2) {
+            r_cur = to_double(m.r);
+            const double dt0 = reference_dt(r_cur, radius_eh(R.camera.bhspin), R.policy.div, R.policy.tol, why);
+            dt = T(dt0);
+            if (dt0 == 0.0 || R.policy.nmax < 2) {
                 // stopped before its next step (reference K = steps), or N < 2
                 // leaves no row pair for the transfer solve
                 if (why == MK_RAY_ACTIVE) why = MK_RAY_MAXSTEPS;
@@ -237,16 +361,16 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
             const mk_request &R = reqs[rq];
-            const double a = R.camera.bhspin;
-            double nw[8], dn[4];
+            const T a = T(R.camera.bhspin);
+            T nw[8], dn[4];
             rk4_step_k1(s, d1, dt, a, nw);
             // next step's first stage, evaluated now: gives r and the metric
             // at the new point for the rule and the sample
-            KerrPoint<double> m;
+            KerrPoint<T> m;
             kerr_accel(nw[1], nw[2], nw[3], nw[4], nw[5], nw[6], nw[7], a, dn[0], dn[1], dn[2], dn[3], m);
             int w1;
-            const double r_new = m.r;
-            const double dtn = reference_dt(r_new, radius_eh(a), R.policy.div, R.policy.tol, w1);
+            const double r_new = to_double(m.r);
+            const double dtn = reference_dt(r_new, radius_eh(R.camera.bhspin), R.policy.div, R.policy.tol, w1);
             if (dtn == 0.0) {
                 // the step is rejected and the ray stays frozen (geodesics.py:263-267)
                 finish_ray(R, pix, I, steps, w1, nsamples, max_tau, ws);
@@ -256,11 +380,14 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
                 for (int i = 0; i < 8; i++) s[i] = nw[i];
 #pragma unroll
                 for (int i = 0; i < 4; i++) d1[i] = dn[i];
-                const double dt_used = dt;
-                dt = dtn;
+                const double dt_used = to_double(dt);
+                dt = T(dtn);
                 ++steps;
                 ++fp64_steps;
-                sample_fp64(R, snaps[R.snapshot], s, m, dt_used, I, P, nsamples, max_tau);
+                if constexpr (SRC == SRC_CAMERA)
+                    sample_fp64(R, snaps[R.snapshot], s, m, dt_used, I, P, nsamples, max_tau);
+                else  // mixed form: FP64 (or pair) geodesic, FP32 emission, FP64 sums
+                    sample_f32_at(R, snaps[R.snapshot], sf, s, m, dt_used, I, P, sc, nsamples, max_tau);
                 // trajectory rows stop at N-1: step N-1 never reaches the solve
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray(R, pix, I, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
@@ -271,7 +398,7 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
                     if ((long long)slot < capacity) {
                         RayRecord &q = q32[slot];
 #pragma unroll
-                        for (int i = 0; i < 8; i++) q.s[i] = s[i];
+                        for (int i = 0; i < 8; i++) q.s[i] = to_double(s[i]);
 #pragma unroll
                         for (int ch = 0; ch < MK_MAX_NU; ch++) { q.I[ch] = I[ch]; q.P[ch] = P[ch]; }
                         q.max_tau = max_tau;
@@ -289,65 +416,6 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
         }
     }
     if (SRC == SRC_QUEUE && fp64_steps) atomicAdd(&ws->steps_fp64, (unsigned long long)fp64_steps);
-}
-
-// ------------------------------------------------------------------ FP32
-// emission of one sample in float (mixed form); I is a compensated sum
-__device__ __forceinline__ void sample_f32(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
-                                           const float s[8], const KerrPoint<float> &m, float dt_used,
-                                           float I[MK_MAX_NU],
-                                           float Ic[MK_MAX_NU], float P[MK_MAX_NU], const SynchroF32 sc[MK_MAX_NU],
-                                           int &nsamples, float &max_tau) {
-    CellPosF c;
-    if (!locate_f32(sv, sf, s[1], s[2], s[3], c)) return;
-    ++nsamples;
-    float prim[8];
-    trilinear8_f32(sv, c, prim);
-    const FluidF32 fs = fluid_frame_f32(prim, m, s + 4, (float)R.cos_fallback_pitch);
-    const float bsq = fs.b * fs.b;
-    const float beta = fs.u * (float)(R.fluid_gamma - 1.) / bsq * 2.0f;
-    const float sigma = bsq / fs.dens;
-    const float b2 = beta * beta;
-    const float T_ratio = ((float)R.r_high * b2 + (float)R.r_low) / (1.0f + b2);
-    const float gem1 = (float)R.electron_gamma_m1, gim1 = (float)R.ion_gamma_m1;
-    // Theta_e = (MP/ME) u gem1 gim1 / (dens (gim1 + gem1 T_ratio))
-    const float Th = (float)(MP / ME) * fs.u * gem1 * gim1 / (fs.dens * (gim1 + gem1 * T_ratio));
-    const float Ne = (float)R.Ne_unit * fs.dens;
-    const float Bg = (float)R.B_unit * fs.b;
-    const float sin_p = sqrtf(fmaxf(0.0f, 1.0f - fs.cos_pitch * fs.cos_pitch));
-    const float th2 = Th * Th;
-    // nus in Hz; nu' = -k.u (observed frequency rescaled to 1)
-    const float nus = (float)(TWO_NINTHS * EE / TWO_PI_ME_CL) * Bg * th2 * sin_p;
-    const float nup = -fs.kdotu;
-    const float w = -dt_used * (float)R.L_unit;
-    const bool cut = sigma > (float)R.sigma_cut || Th < 0.3f;
-#pragma unroll
-    for (int ch = 0; ch < MK_MAX_NU; ch++) {
-        if (ch < R.nnu) {
-            const float nusp = nus * sc[ch].inv_nu;  // nus / nu_obs
-            const float X = nup / nusp;
-            const float x3 = cbrtf(X);
-            const float term = sqrtf(X) + (float)C2_11_12 * sqrtf(x3);
-            // emissivity / nu'^2 (invariant, rescaled): k_em folds
-            // sqrt2 pi EE^2 / (3 CL) and nu_obs
-            float em = Ne * sc[ch].k_em * nusp * term * term / (2.0f * th2) * __expf(-x3) / (nup * nup);
-            if (X > 1.e12f || cut) em = 0.0f;
-            const float bx = sc[ch].k_bx * nup / Th;
-            const float bden = bx < 2.e-3f ? bx / 24.f * (24.f + bx * (12.f + bx * (4.f + bx))) : expm1f(bx);
-            // alpha nu' = (em nu'^2) / B_nu * nu' with B_nu = k_bnu nu'^3 / bden
-            float ab = em * bden / sc[ch].k_bnu;
-            if (isnan(em)) em = 0.0f;
-            if (isnan(ab)) ab = 0.0f;
-            const float tau = w * ab;
-            // Kahan-compensated I += (w em) P
-            const float y = (w * em) * P[ch] - Ic[ch];
-            const float t = I[ch] + y;
-            Ic[ch] = (t - I[ch]) - y;
-            I[ch] = t;
-            P[ch] *= (1.0f - tau);
-            max_tau = fmaxf(max_tau, tau);
-        }
-    }
 }
 
 __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix, const float I[MK_MAX_NU],
@@ -515,7 +583,8 @@ using namespace mk;
 
 extern "C" size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision) {
     if (total_rays < 0) return 0;
-    if (precision == MK_MIXED) return WS_HEADER + 2 * (size_t)total_rays * sizeof(RayRecord);
+    if (precision == MK_MIXED || precision == MK_MIXED_DF)
+        return WS_HEADER + 2 * (size_t)total_rays * sizeof(RayRecord);
     return WS_HEADER;
 }
 
@@ -524,8 +593,8 @@ extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
                          void *workspace_dev, size_t workspace_bytes, void *stream) {
     MK_REQUIRE(reqs_dev && snaps_dev && workspace_dev, MK_ERR_ARG, "mk_render: null pointer");
     MK_REQUIRE(nreq > 0 && nsnap > 0 && total_rays >= 0, MK_ERR_ARG, "mk_render: bad sizes");
-    MK_REQUIRE(precision == MK_FP64 || precision == MK_MIXED, MK_ERR_ARG, "mk_render: unknown precision %d",
-               (int)precision);
+    MK_REQUIRE(precision == MK_FP64 || precision == MK_MIXED || precision == MK_MIXED_DF, MK_ERR_ARG,
+               "mk_render: unknown precision %d", (int)precision);
     const size_t need = mk_render_workspace_bytes(total_rays, precision);
     MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render: workspace of %zu bytes, need %zu",
                workspace_bytes, need);
@@ -554,8 +623,11 @@ extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     // units of a few SMs (one FP64 warp instruction occupies a
     // sub-partition's FP64 unit for tens of cycles on this part).
     {
-        unsigned grid = (unsigned)device_sm_count() * 4;
-        render_fp64_kernel<SRC_QUEUE><<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
+        const unsigned grid = (unsigned)device_sm_count() * 4;
+        if (precision == MK_MIXED)
+            render_fp64_kernel<SRC_QUEUE, double><<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
+        else
+            render_fp64_kernel<SRC_QUEUE, dd><<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
     }
     MK_LAUNCHED("render_fp64_kernel (queue)");
     render_f32_kernel<SRC_QUEUE>

@@ -21,7 +21,7 @@ from .geodesics import camera_pixels, make_camera, step_policy
 
 __all__ = ["make_image", "RenderRequest", "PreparedRender", "render_requests", "image_flux_jy"]
 
-PRECISIONS = {"fp64": _lib.MK_FP64, "mixed": _lib.MK_MIXED}
+PRECISIONS = {"fp64": _lib.MK_FP64, "mixed": _lib.MK_MIXED, "mixed_df": _lib.MK_MIXED_DF}
 
 
 @dataclass

@@ -23,30 +23,32 @@ def medium_model():
     return AthenakFluidModel(arrs, 0.94, fluid_gamma=13. / 9)
 
 
-def _pair(model, **kw):
+def _pair(model, precision, **kw):
     from mahakala_gb300.images import RenderRequest, render_requests
     r64 = RenderRequest(model, **kw)
     rmx = RenderRequest(model, **kw)
     i64 = render_requests([r64], precision="fp64", with_steps=True)[0].cpu().numpy()
-    imx = render_requests([rmx], precision="mixed", with_steps=True)[0].cpu().numpy()
+    imx = render_requests([rmx], precision=precision, with_steps=True)[0].cpu().numpy()
     return i64, imx, r64.out["status"].cpu().numpy(), rmx.out["status"].cpu().numpy()
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
 @pytest.mark.parametrize("spin,inc,rh", [(0.94, 17.0, 40.0), (0.5, 60.0, 10.0), (0.0, 85.0, 1.0)])
-def test_mixed_matches_fp64(cuda, medium_model, spin, inc, rh):
+def test_mixed_matches_fp64(cuda, medium_model, precision, spin, inc, rh):
     from mahakala_gb300 import configs, metrics
     kw = dict(camera_inclination=inc, mass_scale=configs.mass_scale_for(rh), M_bh=6.5e9 * 1.989e33, r_high=rh,
               observing_frequency=230e9, fov=50.0, resolution=48, max_nsteps=8192, bhspin=spin)
-    i64, imx, s64, smx = _pair(medium_model, **kw)
+    i64, imx, s64, smx = _pair(medium_model, precision, **kw)
     assert i64.max() > 0 and np.all(np.isfinite(imx))
     m = metrics.compare(imx, i64, smx, s64, 50.0)
-    print(spin, inc, rh, m)
+    print(precision, spin, inc, rh, m)
     assert m["flux_rel_err"] <= FLUX_TOL
     assert m["max_pixel_rel_err"] <= PIX_TOL
     assert abs(m["shadow_diameter"] - m["shadow_diameter_fp64"]) <= 2 * 50.0 / 48
 
 
-def test_mixed_multifrequency_and_batch(cuda, medium_model):
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+def test_mixed_multifrequency_and_batch(cuda, medium_model, precision):
     """Three frequencies in one mixed pass, and a batch of requests, each
     within the bar of its FP64 render."""
     from mahakala_gb300 import configs, metrics
@@ -56,7 +58,7 @@ def test_mixed_multifrequency_and_batch(cuda, medium_model):
                 mass_scale=1e28, r_high=40.0, max_nsteps=8192),
            dict(camera_inclination=70.0, observing_frequency=345e9, resolution=24, fov=40.0, bhspin=0.5,
                 mass_scale=configs.mass_scale_for(5.0), r_high=5.0, max_nsteps=8192)]
-    mixed = render_requests([RenderRequest(medium_model, **k) for k in kws], precision="mixed")
+    mixed = render_requests([RenderRequest(medium_model, **k) for k in kws], precision=precision)
     for k, imx in zip(kws, mixed):
         i64 = render_requests([RenderRequest(medium_model, **k)], precision="fp64")[0].cpu().numpy()
         imx = imx.cpu().numpy()
@@ -66,11 +68,13 @@ def test_mixed_multifrequency_and_batch(cuda, medium_model):
             assert metrics.max_pixel_rel_err(imx[c], i64[c]) <= PIX_TOL
 
 
-def test_mixed_hands_rays_to_fp64(cuda, medium_model):
-    """Captured rays and photon-ring rays are integrated in FP64 near the hole."""
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+def test_mixed_hands_rays_to_fp64(cuda, medium_model, precision):
+    """Captured rays and photon-ring rays are integrated in FP64 (or pairs)
+    near the hole."""
     from mahakala_gb300.images import PreparedRender, RenderRequest
     prep = PreparedRender([RenderRequest(medium_model, camera_inclination=17.0, resolution=32, fov=50.0,
-                                         max_nsteps=8192)], precision="mixed")
+                                         max_nsteps=8192)], precision=precision)
     prep.launch()
     to64, back32, steps64 = prep.precision_split()
     steps, _ = prep.work_totals()
