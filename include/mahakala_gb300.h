@@ -246,6 +246,23 @@ int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
               const mk_snapshot_view *snaps_dev, int32_t nsnap, int32_t precision,
               void *workspace_dev, size_t workspace_bytes, void *stream);
 
+/* Allocation-free render.  No counterpart in the reference (Mahakala is
+   Python and never manages device scratch).  For callers that cannot give
+   this library device memory -- a plugin confined to its host framework's
+   fixed memory pool, code that must not call cudaMalloc mid-render -- this
+   is mk_render with its scratch in a static device array of
+   MK_NOALLOC_WORKSPACE_BYTES that every GPU loading the library holds until
+   exit.  The caller still passes requests, snapshots and images.  Limit:
+   any ray count in MK_FP64; at most MK_NOALLOC_MAX_MIXED_RAYS rays per call
+   in the mixed forms (larger jobs return MK_ERR_LIMIT).  The first call on
+   a device looks the array up (cudaGetSymbolAddress) and should come before
+   any stream capture.  All calls share the array: calls that overlap on the
+   GPU race. */
+#define MK_NOALLOC_WORKSPACE_BYTES (16u << 20)
+#define MK_NOALLOC_MAX_MIXED_RAYS ((MK_NOALLOC_WORKSPACE_BYTES - 256u) / 320u)
+int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
+                      const mk_snapshot_view *snaps_dev, int32_t nsnap, int32_t precision, void *stream);
+
 /* ------------------------------------------------------------ probes */
 /* FMA throughput probe (no reference counterpart): blocks x threads
    threads each run iters x 8 dependent-chain FMAs in FP64

@@ -22,6 +22,8 @@ MK_FP64, MK_MIXED, MK_MIXED_DF = 0, 1, 2
 MK_POLICY_REFERENCE, MK_POLICY_FIXED = 0, 1
 MK_CAMERA_GRID, MK_CAMERA_EQUATOR = 0, 1
 MK_MAX_NU = 4
+NOALLOC_WORKSPACE_BYTES = 16 << 20
+NOALLOC_MAX_MIXED_RAYS = (NOALLOC_WORKSPACE_BYTES - 256) // 320
 MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_TO_FP32, MK_WS_STEPS_FP64 = 1, 2, 3, 4, 6, 8
 
 
@@ -80,6 +82,7 @@ SIGNATURES = {
     "mk_attenuated_emissivity": (_c.c_int, [_VP, _VP, _VP, _I64, _I64, _D, _VP, _VP]),
     "mk_render_workspace_bytes": (_SZ, [_I64, _I32]),
     "mk_render": (_c.c_int, [_VP, _I32, _I64, _VP, _I32, _I32, _VP, _SZ, _VP]),
+    "mk_render_noalloc": (_c.c_int, [_VP, _I32, _I64, _VP, _I32, _I32, _VP]),
     "mk_sizeof": (_SZ, [_c.c_char_p]),
     "mk_probe_fma": (_c.c_int, [_I32, _I32, _I32, _I64, _VP, _VP]),
 }

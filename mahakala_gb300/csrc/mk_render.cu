@@ -636,3 +636,6 @@ extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     MK_LAUNCHED("render_f32_kernel (queue)");
     return MK_OK;
 }
+
+// the allocation-free entry point sizes its static workspace from these
+static_assert(mk::WS_HEADER == 256 && sizeof(mk::RayRecord) == 160, "MK_NOALLOC_MAX_MIXED_RAYS assumes 256 + 320 B/ray");
