@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--workload", default="render256", choices=["render256", "stress1024"])
     p.add_argument("--cpu-sample-rays", type=int, default=0, help="rays per CPU baseline sample (0 = auto)")
     p.add_argument("--resolution", type=int, default=0, help="override the image size (profiling small cases)")
+    p.add_argument("--serving", type=int, default=60,
+                   help="requests in the served Poisson stream (0 = skip the serving measurement)")
     p.add_argument("--quick", action="store_true",
                    help="device timing only: skip the FMA probes, the end-to-end pass and the CPU baseline")
     return p.parse_args()
@@ -231,6 +233,40 @@ def time_render(torch, prep, stream, steps, warmup, flush, barrier):
     return [a.elapsed_time(b) * 1e-3 for a, b in ev]
 
 
+def run_serving(torch, model0, n, precisions):
+    """Config-4 stream: Poisson arrivals at 20/s over two resident snapshots
+    (seeds 0 and 1), mixed resolutions/spins/inclinations/frequencies/R_high,
+    continuous batching over two CUDA-graph slots.  Per form: p50/p99
+    latency, served rays/s, and the p99 of each request's latency divided by
+    its isolated single-image render time."""
+    from mahakala_gb300 import configs
+    from mahakala_gb300.grmhd.athenak import AthenakFluidModel
+    from mahakala_gb300.serving import (DeviceExecutor, Scheduler, isolated_times, latency_report, poisson_stream,
+                                        serve_stream)
+    c = configs.SERVING
+    model1 = AthenakFluidModel(c["snapshots"][1].build(), 0.94, fluid_gamma=13. / 9)
+    models = [model0, model1]
+    out = {"requests": n, "rate_hz": c["rate_hz"], "snapshots": "256^3-cell synthetic, seeds 0 and 1",
+           "slots": 2, "buckets": None}
+    for form in precisions:
+        arrivals, reqs = poisson_stream(models, n, rate_hz=c["rate_hz"], seed=c["seed"])
+        ex = DeviceExecutor(models, precision=form, nslots=2)
+        out["buckets"] = list(ex.buckets)
+        sched = Scheduler(ex, hbm_budget=ex.resident_bytes + (8 << 30))
+        torch.cuda.synchronize()
+        tickets, wall = serve_stream(sched, arrivals, reqs)
+        iso, _ = isolated_times(reqs, form)
+        rep = latency_report(tickets, wall, isolated={t.id: iso[i] for i, t in enumerate(tickets)})
+        rep["isolated_ms_p50"] = 1e3 * float(np.percentile(iso, 50))
+        rep["isolated_ms_p99"] = 1e3 * float(np.percentile(iso, 99))
+        rep["batches"] = len(sched.batches)
+        rep["mean_requests_per_batch"] = float(np.mean([b["requests"] for b in sched.batches]))
+        out[form] = rep
+        del ex, sched
+        torch.cuda.empty_cache()
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -279,11 +315,15 @@ def main():
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             t_step = float(t.item())
         steps_total, samples_total = prep.work_totals()
-        split = prep.precision_split() if form == "mixed" else (0, 0, steps_total)
+        split = prep.precision_split() if form.startswith("mixed") else (0, 0, steps_total)
         res[form] = dict(prep=prep, req=req, t_step=t_step, steps=steps_total, samples=samples_total,
                          split=split, image=prep.images[0].clone(), status=req.out["status"].clone(),
                          max_tau=prep.max_step_optical_depth())
     clocks = clocks_summary(proc, fh, cpath, local) if rank == 0 else None
+
+    serving = None
+    if args.serving and not args.quick and args.workload == "render256":
+        serving = run_serving(torch, model, args.serving, [f for f in ("mixed", "fp64") if f in forms])
 
     # end to end through the public API: host request in, NumPy image out
     e2e_times = []
@@ -371,6 +411,7 @@ def main():
         "e2e": {"value": world * rays / e2e_t, "unit": "rays/s", "h2d_bytes_per_step": len(res[head]["prep"].table_bytes),
                 "d2h_bytes_per_step": int(rays * nnu * 8),
                 "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
+        "serving": serving,
         "gpu_launches": args.steps * (1 if head == "fp64" else 3),
         "clocks": clocks,
         "snapshot_build_s": t_gen,

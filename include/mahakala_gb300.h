@@ -246,6 +246,23 @@ int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
               const mk_snapshot_view *snaps_dev, int32_t nsnap, int32_t precision,
               void *workspace_dev, size_t workspace_bytes, void *stream);
 
+/* A render job whose size lives in device memory, so one launch sequence
+   can be captured once (a CUDA graph per size bucket) and replayed with
+   new requests: the replay copies the header and the request table in,
+   then runs the render.  total_rays <= the max_rays the sequence was
+   built for. */
+typedef struct {
+    int32_t nreq, nsnap;
+    int64_t total_rays;
+} mk_job;
+
+/* mk_render with nreq and total_rays read from job_dev on the device;
+   grids and workspace (mk_render_workspace_bytes(max_rays, precision)) are
+   sized for max_rays. */
+int mk_render_job(const mk_job *job_dev, const mk_request *reqs_dev, const mk_snapshot_view *snaps_dev,
+                  int32_t precision, int64_t max_rays, void *workspace_dev, size_t workspace_bytes,
+                  void *stream);
+
 /* Allocation-free render.  No counterpart in the reference (Mahakala is
    Python and never manages device scratch).  For callers that cannot give
    this library device memory -- a plugin confined to its host framework's
@@ -262,6 +279,11 @@ int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
 #define MK_NOALLOC_MAX_MIXED_RAYS ((MK_NOALLOC_WORKSPACE_BYTES - 256u) / 320u)
 int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
                       const mk_snapshot_view *snaps_dev, int32_t nsnap, int32_t precision, void *stream);
+
+/* Process-wide tuning knobs (no reference counterpart).
+   "fp64_rays_per_warp" (1, 2, 4, 8, 16 or 32; default 32): rays each warp
+   of the mixed form's FP64 phase carries. */
+int mk_set_tuning(const char *name, int64_t value);
 
 /* ------------------------------------------------------------ probes */
 /* FMA throughput probe (no reference counterpart): blocks x threads

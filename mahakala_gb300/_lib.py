@@ -59,6 +59,10 @@ class Request(_c.Structure):
                 ("ray_offset", _I64)]
 
 
+class Job(_c.Structure):
+    _fields_ = [("nreq", _I32), ("nsnap", _I32), ("total_rays", _I64)]
+
+
 # name -> (restype, argtypes); the declarations of include/mahakala_gb300.h
 SIGNATURES = {
     "mk_version": (_c.c_char_p, []),
@@ -83,8 +87,10 @@ SIGNATURES = {
     "mk_render_workspace_bytes": (_SZ, [_I64, _I32]),
     "mk_render": (_c.c_int, [_VP, _I32, _I64, _VP, _I32, _I32, _VP, _SZ, _VP]),
     "mk_render_noalloc": (_c.c_int, [_VP, _I32, _I64, _VP, _I32, _I32, _VP]),
+    "mk_render_job": (_c.c_int, [_VP, _VP, _VP, _I32, _I64, _VP, _SZ, _VP]),
     "mk_sizeof": (_SZ, [_c.c_char_p]),
     "mk_probe_fma": (_c.c_int, [_I32, _I32, _I32, _I64, _VP, _VP]),
+    "mk_set_tuning": (_c.c_int, [_c.c_char_p, _I64]),
 }
 
 _LIB = None

@@ -32,6 +32,8 @@
 //   rate is 1/64 of FP32, one FP64 lane would stall the other 31.  The
 //   intensity accumulates with a compensated (Kahan) FP32 sum and the
 //   transmission product in FP32; both move to FP64 with the ray.
+#include <string.h>
+
 #include "mk_common.cuh"
 #include "mk_dd.cuh"
 #include "mk_fluid.cuh"
@@ -41,6 +43,11 @@ namespace mk {
 constexpr int RENDER_THREADS = 128;
 constexpr double R_FP64 = 3.0;
 constexpr double R_TURN = 6.0;
+
+// rays per warp in the mixed form's FP64 phase (mk_set_tuning
+// "fp64_rays_per_warp"): 32 fills every lane; fewer rays per warp shorten
+// each warp's FP64 chain when the FP64 unit processes only active lanes
+static int g_fp64_rays_per_warp = 32;
 
 // launch scratch: counters and work totals, then (mixed form) two queues
 struct RenderWorkspace {
@@ -289,8 +296,14 @@ template <int SRC, typename T = double>
 __global__ void __launch_bounds__(RENDER_THREADS)
 render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
                    const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64,
-                   RayRecord *q32, long long capacity) {
+                   RayRecord *q32, long long capacity, int lane_stride, const mk_job *job) {
+    if (job) {  // request count and ray total from the device (graph replays)
+        nreq = job->nreq;
+        total_camera = job->total_rays;
+    }
     unsigned long long *counter = SRC == SRC_CAMERA ? &ws->counter : &ws->q64_next;
+    // lanes not on the stride never take work and stay masked off
+    const bool lane_works = ((threadIdx.x & 31) % lane_stride) == 0;
     const long long total =
         SRC == SRC_CAMERA ? total_camera : (long long)*(volatile unsigned long long *)&ws->q64_count;
     bool active = false, exhausted = false;
@@ -303,8 +316,9 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
     SnapF32 sf;
 
     for (;;) {
-        const long long idx = fetch(!active && !exhausted, counter, total);
+        const long long idx = fetch(lane_works && !active && !exhausted, counter, total);
         if (idx == -1) exhausted = true;
+        if (!lane_works) exhausted = true;
         if (idx >= 0) {
             if (SRC == SRC_CAMERA) {
                 ray = idx;
@@ -435,7 +449,11 @@ template <int SRC>
 __global__ void __launch_bounds__(RENDER_THREADS)
 render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
                   const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64, RayRecord *q32,
-                  long long capacity) {
+                  long long capacity, const mk_job *job) {
+    if (job) {
+        nreq = job->nreq;
+        total_camera = job->total_rays;
+    }
     unsigned long long *counter = SRC == SRC_CAMERA ? &ws->counter : &ws->q32_next;
     const long long total =
         SRC == SRC_CAMERA ? total_camera : (long long)*(volatile unsigned long long *)&ws->q32_count;
@@ -577,9 +595,19 @@ static unsigned persistent_grid(int per_sm, int64_t rays) {
     return (unsigned)(grid < 1 ? 1 : grid);
 }
 
-}  // namespace mk
 
-using namespace mk;
+
+
+extern "C" int mk_set_tuning(const char *name, int64_t value) {
+    MK_REQUIRE(name, MK_ERR_ARG, "mk_set_tuning: null name");
+    if (!strcmp(name, "fp64_rays_per_warp")) {
+        MK_REQUIRE(value == 1 || value == 2 || value == 4 || value == 8 || value == 16 || value == 32, MK_ERR_ARG,
+                   "mk_set_tuning: fp64_rays_per_warp must be a power of two in 1..32");
+        g_fp64_rays_per_warp = (int)value;
+        return MK_OK;
+    }
+    MK_REQUIRE(false, MK_ERR_ARG, "mk_set_tuning: unknown parameter '%s'", name);
+}
 
 extern "C" size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision) {
     if (total_rays < 0) return 0;
@@ -587,6 +615,53 @@ extern "C" size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precisio
         return WS_HEADER + 2 * (size_t)total_rays * sizeof(RayRecord);
     return WS_HEADER;
 }
+
+static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays, int64_t max_rays,
+                         const mk_job *job_dev, const mk_snapshot_view *snaps_dev, int32_t precision,
+                         void *workspace_dev, cudaStream_t st) {
+    MK_CUDA(cudaMemsetAsync(workspace_dev, 0, WS_HEADER, st));
+    if (max_rays == 0) return MK_OK;
+    RenderWorkspace *ws = (RenderWorkspace *)workspace_dev;
+    if (precision == MK_FP64) {
+        const unsigned grid = persistent_grid(blocks_per_sm(render_fp64_kernel<SRC_CAMERA>, 0), max_rays);
+        render_fp64_kernel<SRC_CAMERA><<<grid, RENDER_THREADS, 0, st>>>(reqs_dev, nreq, (long long)total_rays,
+                                                                        snaps_dev, ws, nullptr, nullptr, 0, 1,
+                                                                        job_dev);
+        MK_LAUNCHED("render_fp64_kernel");
+        return MK_OK;
+    }
+    RayRecord *q64 = (RayRecord *)((char *)workspace_dev + WS_HEADER);
+    RayRecord *q32 = q64 + max_rays;
+    const long long cap = (long long)max_rays;
+    render_f32_kernel<SRC_CAMERA>
+        <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA>, 1), max_rays), RENDER_THREADS, 0, st>>>(
+            reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev);
+    MK_LAUNCHED("render_f32_kernel (camera)");
+    // The queues' sizes are only known on the device: persistent grids.
+    // Phase B runs one warp per block, 4 blocks per SM: the few FP64 rays
+    // spread over every SM sub-partition instead of queuing on the FP64
+    // units of a few SMs (one FP64 warp instruction occupies a
+    // sub-partition's FP64 unit for tens of cycles on this part).
+    {
+        const int per_warp = g_fp64_rays_per_warp;
+        const int stride = 32 / per_warp;
+        const unsigned grid = (unsigned)device_sm_count() * (per_warp >= 32 ? 4 : 16);
+        if (precision == MK_MIXED)
+            render_fp64_kernel<SRC_QUEUE, double>
+                <<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, stride, job_dev);
+        else
+            render_fp64_kernel<SRC_QUEUE, dd>
+                <<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, stride, job_dev);
+    }
+    MK_LAUNCHED("render_fp64_kernel (queue)");
+    render_f32_kernel<SRC_QUEUE>
+        <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE>, 3), max_rays), RENDER_THREADS, 0, st>>>(
+            reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev);
+    MK_LAUNCHED("render_f32_kernel (queue)");
+    return MK_OK;
+}
+
+}  // namespace mk
 
 extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
                          const mk_snapshot_view *snaps_dev, int32_t nsnap, int32_t precision,
@@ -599,42 +674,23 @@ extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render: workspace of %zu bytes, need %zu",
                workspace_bytes, need);
     MK_REQUIRE(((uintptr_t)workspace_dev & 15) == 0, MK_ERR_ARG, "mk_render: workspace not 16-byte aligned");
-    cudaStream_t st = as_stream(stream);
-    MK_CUDA(cudaMemsetAsync(workspace_dev, 0, WS_HEADER, st));
-    if (total_rays == 0) return MK_OK;
-    RenderWorkspace *ws = (RenderWorkspace *)workspace_dev;
-    if (precision == MK_FP64) {
-        const unsigned grid = persistent_grid(blocks_per_sm(render_fp64_kernel<SRC_CAMERA>, 0), total_rays);
-        render_fp64_kernel<SRC_CAMERA><<<grid, RENDER_THREADS, 0, st>>>(reqs_dev, nreq, (long long)total_rays,
-                                                                        snaps_dev, ws, nullptr, nullptr, 0);
-        MK_LAUNCHED("render_fp64_kernel");
-        return MK_OK;
-    }
-    RayRecord *q64 = (RayRecord *)((char *)workspace_dev + WS_HEADER);
-    RayRecord *q32 = q64 + total_rays;
-    const long long cap = (long long)total_rays;
-    render_f32_kernel<SRC_CAMERA>
-        <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA>, 1), total_rays), RENDER_THREADS, 0, st>>>(
-            reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap);
-    MK_LAUNCHED("render_f32_kernel (camera)");
-    // The queues' sizes are only known on the device: persistent grids.
-    // Phase B runs one warp per block, 4 blocks per SM: the few FP64 rays
-    // spread over every SM sub-partition instead of queuing on the FP64
-    // units of a few SMs (one FP64 warp instruction occupies a
-    // sub-partition's FP64 unit for tens of cycles on this part).
-    {
-        const unsigned grid = (unsigned)device_sm_count() * 4;
-        if (precision == MK_MIXED)
-            render_fp64_kernel<SRC_QUEUE, double><<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
-        else
-            render_fp64_kernel<SRC_QUEUE, dd><<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
-    }
-    MK_LAUNCHED("render_fp64_kernel (queue)");
-    render_f32_kernel<SRC_QUEUE>
-        <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE>, 3), total_rays), RENDER_THREADS, 0, st>>>(
-            reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap);
-    MK_LAUNCHED("render_f32_kernel (queue)");
-    return MK_OK;
+    return mk::launch_render(reqs_dev, nreq, total_rays, total_rays, nullptr, snaps_dev, precision, workspace_dev,
+                             mk::as_stream(stream));
+}
+
+extern "C" int mk_render_job(const mk_job *job_dev, const mk_request *reqs_dev, const mk_snapshot_view *snaps_dev,
+                             int32_t precision, int64_t max_rays, void *workspace_dev, size_t workspace_bytes,
+                             void *stream) {
+    MK_REQUIRE(job_dev && reqs_dev && snaps_dev && workspace_dev, MK_ERR_ARG, "mk_render_job: null pointer");
+    MK_REQUIRE(max_rays >= 0, MK_ERR_ARG, "mk_render_job: negative max_rays");
+    MK_REQUIRE(precision == MK_FP64 || precision == MK_MIXED || precision == MK_MIXED_DF, MK_ERR_ARG,
+               "mk_render_job: unknown precision %d", (int)precision);
+    const size_t need = mk_render_workspace_bytes(max_rays, precision);
+    MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render_job: workspace of %zu bytes, need %zu",
+               workspace_bytes, need);
+    MK_REQUIRE(((uintptr_t)workspace_dev & 15) == 0, MK_ERR_ARG, "mk_render_job: workspace not 16-byte aligned");
+    return mk::launch_render(reqs_dev, 1, 0, max_rays, job_dev, snaps_dev, precision, workspace_dev,
+                             mk::as_stream(stream));
 }
 
 // the allocation-free entry point sizes its static workspace from these

@@ -1,0 +1,407 @@
+"""Render serving with continuous batching.
+
+Requests (``RenderRequest``) arrive at any time.  The scheduler keeps a FIFO
+of admitted-but-waiting requests and a few *slots*, each a CUDA stream with
+its own device buffers.  Whenever a slot is free it packs the waiting
+requests -- any mix of resolutions, spins, inclinations, frequencies,
+electron models and snapshots -- into ONE persistent render launch, chosen
+from a small set of size *buckets*.  Each (slot, bucket) pair owns a CUDA
+graph captured once: a replay copies the job header and request table from
+pinned host memory and runs the render (``mk_render_job``).  While one
+slot's batch runs, the next arrivals are packed onto another slot, so their
+work overlaps on the device.
+
+Admission is by HBM budget: the snapshots and the slots' buffers are
+resident; a request is admitted when its output buffers fit in what the
+budget leaves, otherwise it waits; a request that can never fit (or that
+is malformed) is rejected at submission.  Latency is measured from
+arrival to the moment its image is in host memory.
+
+The scheduling core (``Scheduler``) is plain Python over an executor
+interface, so its logic is tested on the CPU with a fake executor;
+``DeviceExecutor`` is the GPU implementation.
+"""
+
+import collections
+import ctypes
+import itertools
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+
+BUCKETS = (16384, 65536, 262144, 1048576)
+MAX_REQUESTS_PER_BATCH = 64
+RECORD_BYTES = 320            # mixed-form queue bytes per ray (two 160-byte records)
+
+
+class RequestError(ValueError):
+    """A request was rejected (malformed, or larger than any budget)."""
+
+
+@dataclass
+class Ticket:
+    id: int
+    request: object
+    rays: int
+    out_bytes: int
+    arrival: float
+    admitted: float = None
+    launched: float = None
+    finished: float = None
+    image: np.ndarray = None
+    status: str = "waiting"    # waiting | running | done | failed | cancelled
+    error: str = None
+    batch: int = None
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.arrival
+
+    def done(self):
+        return self.status in ("done", "failed", "cancelled")
+
+
+def validate(req, max_rays):
+    """Reject malformed requests before they reach the device."""
+    res = int(req.resolution)
+    if res <= 0:
+        raise RequestError("resolution must be positive")
+    if res * res > max_rays:
+        raise RequestError(f"{res}x{res} rays exceed the largest bucket ({max_rays})")
+    freqs = req.freqs
+    if not 1 <= len(freqs) <= _lib.MK_MAX_NU or np.any(~np.isfinite(freqs)) or np.any(freqs <= 0):
+        raise RequestError("1..4 positive observing frequencies")
+    a = req.model.bhspin if req.bhspin is None else req.bhspin
+    if not 0.0 <= float(a) < 1.0:
+        raise RequestError("spin must be in [0, 1)")
+    if not (float(req.mass_scale) > 0 and float(req.M_bh) > 0):
+        raise RequestError("mass_scale and M_bh must be positive")
+    if req.model.fluid_gamma is None:
+        raise RequestError("fluid_gamma must be set")
+    if not (float(req.fov) > 0 and int(req.max_nsteps) >= 2):
+        raise RequestError("fov > 0 and max_nsteps >= 2 required")
+
+
+def output_bytes(req):
+    """Device bytes a request's outputs hold while it is in flight."""
+    n = int(req.resolution) ** 2
+    return n * 8 * len(req.freqs) + n * 4 * 2
+
+
+class Scheduler:
+    """Continuous-batching scheduler over an executor.
+
+    executor interface:
+      nslots, buckets, resident_bytes
+      launch(slot, bucket, tickets) -> handle     (asynchronous)
+      poll(handle) -> None while running, else dict(ok=bool, error=str,
+                      images=[...]) with one image per ticket
+    """
+
+    def __init__(self, executor, hbm_budget, max_requests=MAX_REQUESTS_PER_BATCH, clock=time.perf_counter):
+        self.ex = executor
+        self.budget = int(hbm_budget)
+        self.max_requests = int(max_requests)
+        self.clock = clock
+        self.pending = collections.deque()
+        self.slots = [None] * executor.nslots       # (handle, batch_id, tickets) while busy
+        self.in_flight_bytes = 0
+        self.tickets = []
+        self._ids = itertools.count()
+        self._batches = itertools.count()
+        self.batches = []
+        if executor.resident_bytes > self.budget:
+            raise RequestError(f"resident buffers ({executor.resident_bytes} B) exceed the HBM budget")
+
+    @property
+    def free_bytes(self):
+        return self.budget - self.ex.resident_bytes - self.in_flight_bytes
+
+    def submit(self, req, arrival=None):
+        validate(req, max(self.ex.buckets))
+        ob = output_bytes(req)
+        if ob > self.budget - self.ex.resident_bytes:
+            raise RequestError("request outputs exceed the HBM budget")
+        t = Ticket(next(self._ids), req, int(req.resolution) ** 2, ob,
+                   self.clock() if arrival is None else arrival)
+        self.tickets.append(t)
+        self.pending.append(t)
+        return t
+
+    def cancel(self, ticket):
+        """Cancel a request that has not been launched yet."""
+        if ticket.status == "waiting":
+            self.pending.remove(ticket)
+            ticket.status = "cancelled"
+            ticket.finished = self.clock()
+            return True
+        return False
+
+    def _collect(self):
+        for s, busy in enumerate(self.slots):
+            if busy is None:
+                continue
+            handle, bid, tickets = busy
+            res = self.ex.poll(handle)
+            if res is None:
+                continue
+            now = self.clock()
+            for i, t in enumerate(tickets):
+                t.finished = now
+                if res["ok"]:
+                    t.status, t.image = "done", res["images"][i]
+                else:
+                    t.status, t.error = "failed", res["error"]
+                self.in_flight_bytes -= t.out_bytes
+            self.slots[s] = None
+
+    def _pack(self):
+        """FIFO requests that fit one bucket, the request cap and the budget."""
+        cap = max(self.ex.buckets)
+        batch, rays, nbytes = [], 0, 0
+        free = self.free_bytes
+        for t in list(self.pending):
+            if len(batch) >= self.max_requests or rays + t.rays > cap:
+                break
+            if nbytes + t.out_bytes > free:
+                break
+            batch.append(t)
+            rays += t.rays
+            nbytes += t.out_bytes
+        return batch, rays
+
+    def step(self):
+        """Collect finished batches, then launch onto every free slot.
+        Returns True if anything happened."""
+        busy_before = sum(x is not None for x in self.slots)
+        self._collect()
+        progressed = sum(x is not None for x in self.slots) != busy_before
+        for s in range(len(self.slots)):
+            if self.slots[s] is not None or not self.pending:
+                continue
+            batch, rays = self._pack()
+            if not batch:
+                break
+            bucket = min(b for b in self.ex.buckets if b >= rays)
+            now = self.clock()
+            for t in batch:
+                self.pending.remove(t)
+                t.admitted = t.launched = now
+                t.status = "running"
+                self.in_flight_bytes += t.out_bytes
+            bid = next(self._batches)
+            for t in batch:
+                t.batch = bid
+            self.batches.append(dict(id=bid, slot=s, bucket=bucket, rays=rays, requests=len(batch), at=now))
+            try:
+                handle = self.ex.launch(s, bucket, batch)
+            except Exception as e:  # a failed launch fails its batch, not the server
+                handle = dict(error=f"launch failed: {e}")
+            self.slots[s] = (handle, bid, batch)
+            progressed = True
+        return progressed
+
+    def idle(self):
+        return not self.pending and all(x is None for x in self.slots)
+
+    def run_until_idle(self, sleep=1e-4):
+        while not self.idle():
+            if not self.step():
+                time.sleep(sleep)
+
+
+def serve_stream(scheduler, arrivals, requests, sleep=1e-4):
+    """Feed requests at their arrival offsets (seconds from now) in real
+    time and run the scheduler until every request is finished.  Returns
+    the tickets and the wall time."""
+    order = np.argsort(arrivals)
+    t0 = scheduler.clock()
+    tickets = [None] * len(requests)
+    i = 0
+    while i < len(order) or not scheduler.idle():
+        now = scheduler.clock()
+        while i < len(order) and t0 + arrivals[order[i]] <= now:
+            k = order[i]
+            tickets[k] = scheduler.submit(requests[k], arrival=t0 + arrivals[k])
+            i += 1
+        if not scheduler.step():
+            nxt = t0 + arrivals[order[i]] - scheduler.clock() if i < len(order) else sleep
+            time.sleep(min(max(nxt, 0.0), 2e-3) if nxt > 0 else sleep)
+    return tickets, scheduler.clock() - t0
+
+
+def latency_report(tickets, wall, isolated=None):
+    done = [t for t in tickets if t.status == "done"]
+    lat = np.array([t.latency for t in done])
+    rays = sum(t.rays for t in done)
+    out = dict(requests=len(tickets), served=len(done), failed=sum(t.status == "failed" for t in tickets),
+               p50_ms=1e3 * float(np.percentile(lat, 50)) if len(lat) else None,
+               p99_ms=1e3 * float(np.percentile(lat, 99)) if len(lat) else None,
+               max_ms=1e3 * float(lat.max()) if len(lat) else None,
+               rays_per_s=rays / wall if wall > 0 else None, wall_s=wall)
+    if isolated is not None and len(done):
+        slow = np.array([t.latency / isolated[t.id] for t in done])
+        out.update(slowdown_p50=float(np.percentile(slow, 50)), slowdown_p99=float(np.percentile(slow, 99)))
+    return out
+
+
+# --------------------------------------------------------------- device side
+class DeviceExecutor:
+    """GPU executor: ``nslots`` CUDA streams; for each stream and bucket a
+    captured CUDA graph (pinned header/table -> device, mk_render_job) and
+    resident buffers; images come back into pinned host memory."""
+
+    def __init__(self, models, precision="mixed", nslots=2, buckets=BUCKETS, max_requests=MAX_REQUESTS_PER_BATCH,
+                 capture=True):
+        import torch
+
+        from ._device import device
+        from .images import PRECISIONS
+        self.torch = torch
+        self.dev = device()
+        self.precision = PRECISIONS[precision]
+        self.buckets = tuple(sorted(buckets))
+        self.nslots = int(nslots)
+        self.max_requests = int(max_requests)
+        self.models = list(models)
+        self.snap_index = {id(m.snapshot): i for i, m in enumerate(self.models)}
+        self.snaps_dev = torch.cat([m.snapshot.view_dev for m in self.models])
+        lib = _lib.load()
+        self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(self.nslots)]
+        self.slots = []
+        resident = sum(m.snapshot.nbytes for m in self.models)
+        for s in range(self.nslots):
+            per_bucket = {}
+            for b in self.buckets:
+                ws_bytes = lib.mk_render_workspace_bytes(b, self.precision)
+                buf = dict(
+                    job_h=torch.zeros(16, dtype=torch.uint8).pin_memory(),
+                    reqs_h=torch.zeros(self.max_requests * ctypes.sizeof(_lib.Request), dtype=torch.uint8).pin_memory(),
+                    job_d=torch.zeros(16, dtype=torch.uint8, device=self.dev),
+                    reqs_d=torch.zeros(self.max_requests * ctypes.sizeof(_lib.Request), dtype=torch.uint8,
+                                       device=self.dev),
+                    ws=torch.zeros((ws_bytes + 15) // 16 * 2, dtype=torch.int64, device=self.dev),
+                    ws_bytes=ws_bytes, graph=None)
+                resident += buf["ws"].numel() * 8 + buf["reqs_d"].numel() + 16
+                per_bucket[b] = buf
+            self.slots.append(per_bucket)
+        self.resident_bytes = resident
+        self.capture = capture
+        if capture:
+            for s in range(self.nslots):
+                for b in self.buckets:
+                    self._capture(s, b)
+
+    def _enqueue(self, s, b):
+        buf = self.slots[s][b]
+        buf["job_d"].copy_(buf["job_h"], non_blocking=True)
+        buf["reqs_d"].copy_(buf["reqs_h"], non_blocking=True)
+        _lib.call("mk_render_job", buf["job_d"].data_ptr(), buf["reqs_d"].data_ptr(), self.snaps_dev.data_ptr(),
+                  self.precision, b, buf["ws"].data_ptr(), buf["ws_bytes"],
+                  self.torch.cuda.current_stream().cuda_stream)
+
+    def _capture(self, s, b):
+        torch = self.torch
+        g = torch.cuda.CUDAGraph()
+        side = self.streams[s]
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            # the job header says zero rays: the warm-up launch does nothing
+            self._enqueue(s, b)
+        side.synchronize()
+        with torch.cuda.graph(g, stream=side):
+            self._enqueue(s, b)
+        self.slots[s][b]["graph"] = g
+
+    def launch(self, s, b, tickets):
+        torch = self.torch
+        from .images import _fill_request
+        buf = self.slots[s][b]
+        table = (_lib.Request * len(tickets))()
+        images = []
+        offset = 0
+        with torch.cuda.stream(self.streams[s]):
+            for i, t in enumerate(tickets):
+                r = t.request
+                img = torch.empty((len(r.freqs), r.resolution, r.resolution), dtype=torch.float64, device=self.dev)
+                _fill_request(r, table[i], self.snap_index[id(r.model.snapshot)], img, None, None, offset)
+                offset += t.rays
+                images.append(img)
+        raw = bytes(table)
+        buf["reqs_h"][: len(raw)].copy_(torch.frombuffer(bytearray(raw), dtype=torch.uint8))
+        job = _lib.Job(len(tickets), len(self.models), offset)
+        buf["job_h"].copy_(torch.frombuffer(bytearray(bytes(job)), dtype=torch.uint8))
+        stream = self.streams[s]
+        with torch.cuda.stream(stream):
+            if buf["graph"] is not None:
+                buf["graph"].replay()
+            else:
+                self._enqueue(s, b)
+            host = [torch.empty(img.shape, dtype=img.dtype, pin_memory=True) for img in images]
+            for h, img in zip(host, images):
+                h.copy_(img, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        return dict(event=ev, host=host, images=images, error=None)
+
+    def poll(self, handle):
+        if handle.get("error") is not None:
+            return dict(ok=False, error=handle["error"], images=None)
+        if not handle["event"].query():
+            return None
+        return dict(ok=True, error=None, images=[h.numpy().copy() for h in handle["host"]])
+
+
+# ------------------------------------------------------------------ workload
+def poisson_stream(models, n, rate_hz=20.0, seed=2024, resolutions=(64, 128, 256, 512), spins=(0.0, 0.5, 0.94),
+                   inc_range=(10.0, 85.0), freqs=(86e9, 230e9, 345e9), r_high_range=(1.0, 80.0), max_nsteps=8192,
+                   half_fov=25.0):
+    """n requests with exponential inter-arrival gaps (mean 1/rate) and
+    uniformly drawn resolution, spin, inclination, frequency, R_high and
+    snapshot; the density scale follows R_high (configs.mass_scale_for).
+    Returns (arrival offsets in s, requests)."""
+    from .configs import mass_scale_for
+    from .constants import Msun
+    from .images import RenderRequest
+    rng = np.random.Generator(np.random.PCG64(seed))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_hz, n))
+    arrivals -= arrivals[0]
+    reqs = []
+    for _ in range(n):
+        r_high = float(rng.uniform(*r_high_range))
+        reqs.append(RenderRequest(
+            models[int(rng.integers(len(models)))], camera_inclination=float(rng.uniform(*inc_range)),
+            camera_distance=1000.0, mass_scale=mass_scale_for(r_high), M_bh=6.5e9 * Msun, r_high=r_high,
+            observing_frequency=float(freqs[int(rng.integers(len(freqs)))]), fov=2 * half_fov,
+            resolution=int(resolutions[int(rng.integers(len(resolutions)))]), max_nsteps=max_nsteps,
+            bhspin=float(spins[int(rng.integers(len(spins)))])))
+    return arrivals, reqs
+
+
+def isolated_times(requests, precision, repeats=1):
+    """Seconds each request takes rendered alone (one launch, CUDA events),
+    keyed by position; and its image."""
+    import torch
+
+    from .images import PreparedRender, RenderRequest
+    out, images = [], []
+    for r in requests:
+        prep = PreparedRender([RenderRequest(**{k: getattr(r, k) for k in (
+            "model", "camera_inclination", "camera_distance", "mass_scale", "M_bh", "r_high",
+            "observing_frequency", "fov", "resolution", "max_nsteps", "r_low", "bhspin")})], precision=precision)
+        prep.launch()
+        best = None
+        for _ in range(repeats):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            prep.launch()
+            e1.record()
+            e1.synchronize()
+            t = e0.elapsed_time(e1) * 1e-3
+            best = t if best is None else min(best, t)
+        out.append(best)
+        images.append(prep.images[0].cpu().numpy())
+    return out, images
