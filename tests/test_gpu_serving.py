@@ -38,7 +38,8 @@ def test_stream_results_equal_isolated(cuda, models, precision):
     _, alone = isolated_times(reqs, precision)
     for t, ref in zip(tickets, alone):
         assert t.image.shape == ref.shape
-        assert np.array_equal(t.image, ref), f"request {t.id} differs in the mix"
+        assert np.all(np.isfinite(ref)), f"request {t.id}: non-finite pixels (unstable transfer)"
+        assert np.array_equal(t.image, ref, equal_nan=True), f"request {t.id} differs in the mix"
     rep = latency_report(tickets, wall=max(t.finished for t in tickets) - min(t.arrival for t in tickets))
     assert rep["served"] == 12 and rep["p99_ms"] > 0
 
