@@ -105,6 +105,18 @@ def mass_scale_for(r_high):
     return float(10 ** (ly[-1] + slope * (x - lx[-1])))
 
 
+def stable_mass_scale(r_high, inclination=17.0, nu=230e9):
+    """Density scale that keeps the transfer's per-step optical depth below
+    ~1 for any view of the synthetic torus: mass_scale_for(r_high) (set at
+    17 deg, 230 GHz), times 0.1 + 0.9 cos^2(inclination) (edge-on rays
+    cross the dense midplane; the optical depth grows roughly as the fifth
+    power of the density scale, so a few-fold reduction suffices), times
+    min(1, nu / 230 GHz) (absorption grows toward low frequency)."""
+    import numpy as np
+    c = np.cos(np.radians(float(inclination)))
+    return mass_scale_for(r_high) * (0.1 + 0.9 * c * c) * min(1.0, float(nu) / 230e9)
+
+
 RENDER_256 = RenderSpec(snapshot=SNAP_256, bhspin=0.94, inclination=17.0, resolution=256, half_fov=25.0,
                         freqs=(230e9,), max_nsteps=8192, r_high=40.0, mass_scale=MASS_SCALE_256)
 

@@ -361,12 +361,11 @@ def poisson_stream(models, n, rate_hz=20.0, seed=2024, resolutions=(64, 128, 256
                    half_fov=25.0):
     """n requests with exponential inter-arrival gaps (mean 1/rate) and
     uniformly drawn resolution, spin, inclination, frequency, R_high and
-    snapshot.  The density scale follows R_high (configs.mass_scale_for,
-    set for 230 GHz) and falls in proportion to the frequency below 230 GHz,
-    which keeps every transfer step's optical depth in the range where the
-    explicit Euler update stays stable (absorption grows toward low
-    frequency).  Returns (arrival offsets in s, requests)."""
-    from .configs import mass_scale_for
+    snapshot.  The density scale is configs.stable_mass_scale of the
+    request's R_high, inclination and frequency, which keeps every transfer
+    step's optical depth in the range where the explicit Euler update stays
+    stable.  Returns (arrival offsets in s, requests)."""
+    from .configs import stable_mass_scale
     from .constants import Msun
     from .images import RenderRequest
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -378,7 +377,7 @@ def poisson_stream(models, n, rate_hz=20.0, seed=2024, resolutions=(64, 128, 256
         model = models[int(rng.integers(len(models)))]
         inc = float(rng.uniform(*inc_range))
         nu = float(freqs[int(rng.integers(len(freqs)))])
-        ms = mass_scale_for(r_high) * min(1.0, nu / 230e9)
+        ms = stable_mass_scale(r_high, inc, nu)
         reqs.append(RenderRequest(
             model, camera_inclination=inc, camera_distance=1000.0, mass_scale=ms, M_bh=6.5e9 * Msun,
             r_high=r_high, observing_frequency=nu, fov=2 * half_fov,

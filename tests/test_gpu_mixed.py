@@ -79,3 +79,15 @@ def test_mixed_hands_rays_to_fp64(cuda, medium_model, precision):
     to64, back32, steps64 = prep.precision_split()
     steps, _ = prep.work_totals()
     assert to64 > 0 and back32 > 0 and 0 < steps64 < steps
+
+
+def test_sweep_corners_within_bar(cuda, medium_model):
+    """A corner subset of the spin x inclination x R_high sweep at 48x48:
+    every image within the mixed-form bar, every transfer stable."""
+    from mahakala_gb300 import sweep
+    rep = sweep.run(resolution=48, spins=(0.0, 0.94), inclinations=(17.0, 85.0), r_highs=(1.0, 40.0),
+                    model=medium_model)
+    assert rep["images"] == 8
+    for r in rep["rows"]:
+        assert r["max_step_optical_depth"] < 2.0, r
+        assert r["flux_rel_err"] <= FLUX_TOL and r["max_pixel_rel_err"] <= PIX_TOL, r
