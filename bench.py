@@ -1,16 +1,19 @@
 """Throughput benchmark of the per-ray imaging path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--precision fp64|mixed] [--workload render256|stress1024]
+                    [--precision fp64|mixed|mixed_strict|mixed_df|all]
+                    [--workload render256|stress1024]
 
 One "step" is one full render of the workload's image through the fused
 persistent kernels: every ray of the image traced, sampled and solved.
 Default workload (``render256``): render of the seeded 256^3-cell synthetic
 snapshot at 256x256 pixels (a=0.94, 17 deg, 230 GHz, <= 8192 steps), timed
-in both forms -- plain FP64 and mixed FP32/FP64 -- with the mixed form's
-flux and per-pixel error against the FP64 image of the same run.  The
-headline value is the mixed form's rays/s.  Printed on rank 0 as one JSON
-line.
+in every form -- plain FP64 and the mixed FP32/FP64 forms (mixed,
+mixed_strict, mixed_df) -- with each mixed form's flux and per-pixel error
+against the FP64 image of the same run.  The headline value is the mixed
+form's rays/s.  ``--workload stress1024``: the 512^3-cell snapshot at
+1024x1024, three frequencies in one pass, <= 16384 steps.  Printed on rank
+0 as one JSON line.
 
 ``--impl reference`` times the reference algorithm on the host cores
 instead: the C restatement of Mahakala's make_image (oracle/, FP64, all
@@ -50,10 +53,10 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="all", choices=["fp64", "mixed", "mixed_df", "all"],
-                   help="all: time FP64, mixed and mixed_df, headline the mixed form and report each mixed "
+    p.add_argument("--precision", default="all", choices=["fp64", "mixed", "mixed_strict", "mixed_df", "all"],
+                   help="all: time every form, headline the mixed form and report each mixed "
                         "form's error vs FP64")
-    p.add_argument("--workload", default="render256", choices=["render256", "stress1024"])
+    p.add_argument("--workload", default="render256", choices=["render256", "stress1024", "vacuum128"])
     p.add_argument("--cpu-sample-rays", type=int, default=0, help="rays per CPU baseline sample (0 = auto)")
     p.add_argument("--resolution", type=int, default=0, help="override the image size (profiling small cases)")
     p.add_argument("--serving", type=int, default=60,
@@ -176,6 +179,9 @@ def run_reference(args):
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return
+    if args.workload == "vacuum128":
+        run_reference_vacuum(args)
+        return
     spec, desc = workload(args.workload, args.resolution, "fp64")
     arrays = spec.snapshot.build()
     threads = os.cpu_count() or 1
@@ -214,23 +220,67 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_vacuum(args):
+    """Reference arm of the vacuum workload: the C restatement's integrator
+    (reference rule) on all host threads, half of the rays per step."""
+    import oracle
+    from mahakala_gb300 import configs
+    c = configs.VACUUM_SHADOW
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    s0 = oracle.initialize_geodesics_at_camera(c["bhspin"], c["inclination"], c["distance"], -c["half_fov"],
+                                               c["half_fov"], c["resolution"])
+    n = s0.shape[0]
+    times = []
+    for k in range(args.warmup + args.steps):
+        sub = s0[(k % 2)::2]
+        t0 = time.perf_counter()
+        oracle.integrate(sub, c["max_nsteps"], 40.0, 1e-4, c["bhspin"])
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    rays = (n + 1) // 2
+    value = rays * len(times) / sum(times)
+    line = {"metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (camera grid; vacuum)",
+            "config": {"workload": f"vacuum trace {c['resolution']}x{c['resolution']}, reference rule"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "rays/s", "cores": threads, "kind": "port",
+                             "sample": f"{rays} rays per step (alternate halves of the camera grid), "
+                                       f"{threads} OpenMP threads"},
+            "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def time_render(torch, prep, stream, steps, warmup, flush, barrier):
     """W warm-up launches, then K launches each timed by CUDA events on the
-    launching stream with an L2 flush (untimed) before each."""
+    launching stream with an L2 flush (untimed) before each.  The library
+    also records events on that stream around each of the render's kernels
+    (one for FP64, phases A/B/C for the mixed forms); returns the step times
+    (s) and the per-kernel times (s) of every timed step."""
+    import ctypes
+    from mahakala_gb300 import _lib
     for _ in range(max(warmup, 3)):
         prep.launch(stream)
     torch.cuda.synchronize()
     barrier()
-    ev = []
-    for _ in range(steps):
-        flush.fill_(1.0)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        prep.launch(stream)
-        e1.record(stream)
-        ev.append((e0, e1))
+    ev, phases = [], []
+    _lib.call("mk_set_tuning", b"phase_events", 1)
+    try:
+        for _ in range(steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            prep.launch(stream)
+            e1.record(stream)
+            ev.append((e0, e1))
+            ms, n = (ctypes.c_float * 3)(), ctypes.c_int32()
+            _lib.call("mk_render_phase_ms", ms, ctypes.byref(n))   # waits for this step
+            phases.append([ms[i] * 1e-3 for i in range(n.value)])
+    finally:
+        _lib.call("mk_set_tuning", b"phase_events", 0)
     barrier()
-    return [a.elapsed_time(b) * 1e-3 for a, b in ev]
+    return [a.elapsed_time(b) * 1e-3 for a, b in ev], phases
 
 
 def run_serving(torch, model0, n, precisions):
@@ -269,8 +319,159 @@ def run_serving(torch, model0, n, precisions):
     return out
 
 
+def hbm_peak():
+    """Measured copy bandwidth of this GPU model (GB/s) and its source."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback (6.8 TB/s, one earlier GB300 copy measurement)"
+
+
+def sampling_stage(torch, model, spec, flush, stream, rays_per_side=128, reps=3):
+    """The sampling stage alone (get_fluid_scalars_from_geodesics as the
+    standalone mk_fluid_scalars kernel) over the reference's trajectory rows
+    of a rays_per_side^2 camera with the workload's view: every row of every
+    ray, as the reference samples them.  Algorithmic bytes per point: 64 B
+    state read + 40 B written, plus the 8-corner x 8-primitive float32
+    gather (256 B) for points inside the snapshot."""
+    import ctypes
+    from mahakala_gb300 import _lib
+    from mahakala_gb300.geodesics import geodesic_integrator, initialize_geodesics_at_camera
+    s0 = initialize_geodesics_at_camera(spec.bhspin, spec.inclination, spec.camera_distance, -spec.half_fov,
+                                        spec.half_fov, rays_per_side)
+    S, _ = geodesic_integrator(spec.max_nsteps, s0, 40.0, 1e-4, spec.bhspin)
+    nt = S.shape[0]
+    pts = S.reshape(-1, 8)
+    n = pts.shape[0]
+    view = ctypes.byref(model.snapshot.view)
+    blk = torch.empty(n, dtype=torch.int32, device="cuda")
+    prims = torch.empty((n, 8), dtype=torch.float64, device="cuda")
+    _lib.call("mk_fluid_prims", view, pts.data_ptr(), n, prims.data_ptr(), blk.data_ptr(), stream.cuda_stream)
+    inside = int((blk >= 0).sum().item())
+    del prims, blk
+    out = torch.empty((n, 5), dtype=torch.float64, device="cuda")
+    cosf = float(np.cos(np.pi / 3))
+
+    def call():
+        _lib.call("mk_fluid_scalars", view, float(spec.bhspin), pts.data_ptr(), n, cosf, out.data_ptr(),
+                  stream.cuda_stream)
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t = statistics.mean(ts)
+    nbytes = n * (64 + 40) + inside * 256
+    peak, src = hbm_peak()
+    del S, pts, out
+    torch.cuda.empty_cache()
+    return {"kernel": "fluid_scalars_kernel", "bound": "hbm", "rays": rays_per_side ** 2, "rows": nt,
+            "points": n, "in_snapshot": inside, "ms": 1e3 * t, "algorithmic_bytes": nbytes,
+            "achieved": nbytes / t / 1e9, "peak": peak, "unit": "GB/s", "frac": nbytes / t / 1e9 / peak,
+            "peak_source": src, "traffic": None,
+            "note": "algorithmic bytes assume every gather from DRAM; neighbouring samples of a ray share "
+                    "cells, so L2 serves part of them (DRAM traffic from ncu in profiles/)"}
+
+
+def run_vacuum(args):
+    """Config-1 vacuum trace: 128x128 rays, a=0.94, 60 deg, +-10 M, <= 4096
+    steps, end states only (no trajectory rows), under the reference step
+    rule (div 40, tol 1e-4) and the fixed-fraction rule."""
+    import torch
+    from mahakala_gb300 import _lib, build
+    from mahakala_gb300 import configs
+    from mahakala_gb300.geodesics import initialize_geodesics_at_camera, step_policy, trace
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    build.build()
+    _lib.load()
+    c = configs.VACUUM_SHADOW
+    n = c["resolution"] ** 2
+    s0 = initialize_geodesics_at_camera(c["bhspin"], c["inclination"], c["distance"], -c["half_fov"],
+                                        c["half_fov"], c["resolution"])
+    pols = {"reference": step_policy(c["max_nsteps"]),
+            "fixed": step_policy(c["max_nsteps"], kind="fixed", hfrac=c["hfrac"], hmin=c["hmin"], hmax=c["hmax"],
+                                 capture=c["capture"], r_escape=c["r_escape"])}
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    peak64 = measure_fma_peak(torch, _lib.MK_FP64)
+    proc, fh, cpath = clocks_sampler() if rank == 0 else (None, None, None)
+    lines = {}
+    for name, pol in pols.items():
+        for _ in range(max(args.warmup, 3)):
+            r = trace(s0, c["bhspin"], pol)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = trace(s0, c["bhspin"], pol)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        t = statistics.mean(ts)
+        K = r["K"].cpu().numpy().astype(np.int64)
+        steps = int(K.sum())
+        flops = steps * FLOP_PER_STEP
+        # end to end: host initial states in, host end states and step counts out
+        s0_host = s0.cpu().pin_memory()
+        e2e = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rr = trace(s0_host.to("cuda", non_blocking=True), c["bhspin"], pol)
+            _ = rr["state"].cpu(), rr["K"].cpu(), rr["why"].cpu()
+            e2e.append(time.perf_counter() - t0)
+        lines[name] = {"rays_per_s": n / t, "ms_per_step": 1e3 * t, "ray_steps": steps,
+                       "ray_steps_per_s": steps / t, "e2e_rays_per_s": n / statistics.mean(e2e),
+                       "roofline": {"bound": "fp64", "achieved": flops / t / 1e12, "peak": peak64 / 1e12,
+                                    "unit": "TFLOP/s", "frac": flops / t / peak64, "traffic": None,
+                                    "kernel": "integrate_%s_kernel" % ("reference" if name == "reference"
+                                                                        else "fixed")}}
+    clocks = clocks_summary(proc, fh, cpath, local) if rank == 0 else None
+    if rank != 0:
+        return
+    import oracle
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    s0h = s0.cpu().numpy()
+    t0 = time.perf_counter()
+    oracle.integrate(s0h, c["max_nsteps"], 40.0, 1e-4, c["bhspin"])
+    cpu_t = time.perf_counter() - t0
+    head = lines["reference"]
+    line = {"metric": "rays/s", "value": world * head["rays_per_s"], "unit": "rays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": head["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (camera grid; vacuum, no snapshot)",
+            "config": {"workload": f"vacuum trace {c['resolution']}x{c['resolution']}, a={c['bhspin']}, "
+                                   f"i={c['inclination']} deg, +-{c['half_fov']} M, <= {c['max_nsteps']} steps, "
+                                   "end states only (reference rule div 40, tol 1e-4; fixed-fraction rule beside)",
+                       "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write, untimed)",
+                       "parallelism": f"replicas x{world}"},
+            "reference_rule": head, "fixed_rule": lines["fixed"], "roofline": head["roofline"],
+            "cpu_baseline": {"value": n / cpu_t, "unit": "rays/s", "cores": threads, "kind": "port",
+                             "sample": f"all {n} rays, reference rule, oracle C restatement ({cpu_t:.1f} s)"},
+            "e2e": {"value": head["e2e_rays_per_s"], "unit": "rays/s", "h2d_bytes_per_step": n * 64,
+                    "d2h_bytes_per_step": n * (64 + 8),
+                    "api": "mahakala_gb300.geodesics.trace (host initial states -> host end states)"},
+            "gpu_launches": args.steps, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "vacuum128" and args.impl == "ours":
+        run_vacuum(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
@@ -286,7 +487,7 @@ def main():
     from mahakala_gb300.grmhd.athenak import AthenakFluidModel
     from mahakala_gb300.images import PreparedRender, image_flux_jy, make_image
 
-    forms = ["fp64", "mixed", "mixed_df"] if args.precision == "all" else [args.precision]
+    forms = ["fp64", "mixed", "mixed_strict", "mixed_df"] if args.precision == "all" else [args.precision]
     head = "mixed" if "mixed" in forms else forms[0]
     spec, desc = workload(args.workload, args.resolution, head)
     t_gen = time.perf_counter()
@@ -310,18 +511,26 @@ def main():
     for form in forms:
         req = spec.request(model)
         prep = PreparedRender([req], precision=form, with_steps=True)
-        times = time_render(torch, prep, stream, args.steps, args.warmup, flush, barrier)
+        times, phases = time_render(torch, prep, stream, args.steps, args.warmup, flush, barrier)
         t_step = statistics.mean(times)
+        t_phase = [statistics.mean(p[i] for p in phases) for i in range(len(phases[0]))]
         if world > 1:
             t = torch.tensor([t_step], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             t_step = float(t.item())
         steps_total, samples_total = prep.work_totals()
         split = prep.precision_split() if form.startswith("mixed") else (0, 0, steps_total)
-        res[form] = dict(prep=prep, req=req, t_step=t_step, steps=steps_total, samples=samples_total,
+        samples64 = prep.samples_fp64() if form.startswith("mixed") else samples_total
+        res[form] = dict(prep=prep, req=req, t_step=t_step, t_phase=t_phase, steps=steps_total,
+                         zone_run_max=prep.zone_run_max() if form == "mixed" else None,
+                         samples=samples_total, samples64=samples64,
                          split=split, image=prep.images[0].clone(), status=req.out["status"].clone(),
                          max_tau=prep.max_step_optical_depth())
     clocks = clocks_summary(proc, fh, cpath, local) if rank == 0 else None
+
+    sampling = None
+    if args.workload == "stress1024" and not args.quick:
+        sampling = sampling_stage(torch, model, spec, flush, stream)
 
     serving = None
     if args.serving and not args.quick and args.workload == "render256":
@@ -341,21 +550,37 @@ def main():
     L_unit = model.get_units(spec.M_bh, spec.mass_scale)["L_unit"]
 
     def roofline(form):
+        """Roofline of the form's dominant kernel, timed by the CUDA events
+        the library records around each kernel of every timed step."""
         r = res[form]
-        flops = r["steps"] * FLOP_PER_STEP + r["samples"] * (FLOP_PER_SAMPLE + FLOP_PER_EXTRA_NU * (nnu - 1))
-        achieved = flops / r["t_step"]
-        peak = peak64 if form == "fp64" else peak32
-        out = {"bound": "fp64" if form == "fp64" else "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12,
-               "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-               "kernel": "render_fp64_kernel" if form == "fp64" else
-               "render_f32_kernel x2 + render_fp64_kernel (queue) (three launches)",
-               "flop_per_launch": flops,
-               "peak_source": "FMA probe measured in this run (mk_probe_fma); the measured-peak file holds no "
-                              "FP64/FP32 ALU figure",
+        per_sample = FLOP_PER_SAMPLE + FLOP_PER_EXTRA_NU * (nnu - 1)
+        src = ("FMA probe measured in this run (mk_probe_fma); the measured-peak file holds no FP64/FP32 "
+               "ALU figure")
+        if form == "fp64":
+            kernels = [("render_fp64_kernel", "fp64", r["steps"] * FLOP_PER_STEP + r["samples"] * per_sample,
+                        r["t_phase"][0], peak64)]
+        else:
+            to64, back32, steps64 = r["split"]
+            f32 = (r["steps"] - steps64) * FLOP_PER_STEP + (r["samples"] - r["samples64"]) * per_sample
+            # phase A does the FP32 steps up to the hand-off, phase C the rest;
+            # their split is not counted, so both carry the FP32 total over their sum
+            tA, tB, tC = r["t_phase"]
+            kernels = [("render_f32_kernel (phases A+C)", "fp32", f32, tA + tC, peak32),
+                       ("render_fp64_kernel (phase B, FP64 queue)", "fp64",
+                        steps64 * FLOP_PER_STEP + r["samples64"] * per_sample, tB, peak64)]
+        table = [{"kernel": k, "bound": b, "flop": fl, "ms": 1e3 * t, "achieved": fl / t / 1e12 if t else None,
+                  "peak": pk / 1e12, "frac": fl / t / pk if t else None} for k, b, fl, t, pk in kernels]
+        top = max(table, key=lambda e: e["ms"])
+        out = {"bound": top["bound"], "achieved": top["achieved"], "peak": top["peak"], "unit": "TFLOP/s",
+               "frac": top["frac"], "traffic": None, "kernel": top["kernel"], "flop_per_launch": top["flop"],
+               "kernel_ms": top["ms"], "peak_source": src, "kernels": table,
                "peak_fp32_tflops": peak32 / 1e12, "peak_fp64_tflops": peak64 / 1e12}
         if form == "fp64":
             out["traffic_note"] = ("ncu on the 192x192 case: 242 MB DRAM read per launch; the kernel is "
                                    "FP64-pipe bound (profiles/render_fp64_kernel_render192.md)")
+        else:
+            out["note"] = ("phase B is bound by the serial chain of the longest FP64 ray (one FP64 warp "
+                           "instruction per sub-partition at a time), not by FP64 throughput")
         return out
 
     def form_line(form):
@@ -365,6 +590,7 @@ def main():
                 "images_per_s": world * nnu / r["t_step"], "ray_steps_per_s": world * r["steps"] / r["t_step"],
                 "accepted_steps": r["steps"], "samples": r["samples"], "steps_per_ray": r["steps"] / rays,
                 "rays_to_fp64": to64, "rays_back_to_fp32": back32, "steps_in_fp64": steps64,
+                "zone_run_max": r["zone_run_max"],
                 "max_step_optical_depth": r["max_tau"],
                 "flux_jy": [float(x) for x in np.atleast_1d(image_flux_jy(r["image"], spec.fov, spec.distance_cm,
                                                                          L_unit))],
@@ -384,7 +610,8 @@ def main():
     line = {
         "metric": "rays/s", "value": world * rays / t_head, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_head, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f32+f64", "mixed_df": "f32+f32x2"}[head],
+        "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f32+f64", "mixed_strict": "f32+f64",
+                                           "mixed_df": "f32+f32x2"}[head],
         "data": "synthetic (seeded snapshot, no external data)",
         "config": {"workload": desc, "precision": head,
                    "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write, untimed)",
@@ -394,7 +621,7 @@ def main():
     }
     for form in forms:
         line[form] = form_line(form)
-    for form in ("mixed", "mixed_df"):
+    for form in ("mixed", "mixed_strict", "mixed_df"):
         if "fp64" not in res or form not in res:
             continue
         a, b = res[form], res["fp64"]
@@ -414,7 +641,9 @@ def main():
                 "d2h_bytes_per_step": int(rays * nnu * 8),
                 "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
         "serving": serving,
+        "sampling_stage": sampling,
         "gpu_launches": args.steps * (1 if head == "fp64" else 3),
+        "phase_ms": {f: [1e3 * t for t in res[f]["t_phase"]] for f in forms},
         "clocks": clocks,
         "snapshot_build_s": t_gen,
     })

@@ -44,12 +44,17 @@ typedef enum {
     MK_RAY_NAN = 4
 } mk_ray_status;
 
-/* MK_FP64: every operation in binary64.  MK_MIXED: FP32 with binary64 near
-   the hole and at photon-ring turning points.  MK_MIXED_DF: as MK_MIXED but
-   the near-hole geodesic runs in double-float (pairs of FP32, ~1e-13
-   relative) instead of binary64 -- not IEEE FP64, faster on parts whose
-   FP64 rate is a small fraction of FP32. */
-typedef enum { MK_FP64 = 0, MK_MIXED = 1, MK_MIXED_DF = 2 } mk_precision;
+/* MK_FP64: every operation in binary64.
+   MK_MIXED: FP32 arithmetic (ray state as float pairs, Kahan-compensated
+   intensity); near the hole (r < 3 M, or inbound inside 6 M where
+   photon-ring rays turn) the ray state and the intensity sums are binary64
+   and the wavevector is renormalised to null in binary64 on entry, on exit
+   and at every radial turning point; accelerations and emission stay FP32.
+   MK_MIXED_STRICT: as MK_MIXED, but near the hole the whole geodesic step
+   (accelerations included) is binary64.
+   MK_MIXED_DF: as MK_MIXED_STRICT with that step in double-float (pairs of
+   FP32, ~1e-13 relative) instead of binary64 -- not IEEE FP64. */
+typedef enum { MK_FP64 = 0, MK_MIXED = 1, MK_MIXED_DF = 2, MK_MIXED_STRICT = 3 } mk_precision;
 
 typedef enum {
     /* dt = -(r - r_EH)/div, stop (and reject the step) when the next dt
@@ -225,13 +230,17 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
    in-snapshot samples, MK_WS_MAX_TAU the bits of a double, the largest
    per-step optical depth w*alpha of the transfer solve (the reference's
    explicit Euler update is stable below 1), MK_WS_TO_FP64 rays handed to
-   FP64 and MK_WS_STEPS_FP64 steps taken in FP64 (mixed form). */
+   FP64, MK_WS_STEPS_FP64 steps and MK_WS_SAMPLES_FP64 in-snapshot samples
+   taken in FP64 (mixed form), MK_WS_ZONE_RUN_MAX the most steps one ray
+   took in one visit to the near-hole phase (MK_MIXED; its serial chain). */
 #define MK_WS_STEPS 1
 #define MK_WS_SAMPLES 2
 #define MK_WS_MAX_TAU 3
 #define MK_WS_TO_FP64 4
 #define MK_WS_TO_FP32 6
 #define MK_WS_STEPS_FP64 8
+#define MK_WS_SAMPLES_FP64 10
+#define MK_WS_ZONE_RUN_MAX 11
 size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision);
 
 /* make_image (images.py:30-144) for nreq requests in ONE persistent launch
@@ -282,8 +291,22 @@ int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_ra
 
 /* Process-wide tuning knobs (no reference counterpart).
    "fp64_rays_per_warp" (1, 2, 4, 8, 16 or 32; default 32): rays each warp
-   of the mixed form's FP64 phase carries. */
+   of the mixed form's FP64 phase carries.
+   "fp64_zone" (0 or 1; default 1): 0 keeps every ray of the mixed forms in
+   FP32 to its end, with no FP64 phase (measures what that phase buys).
+   "f32_blocks_per_sm" (3 or 4; default 4): the FP32 phases' kernels
+   compiled for 3 resident blocks per SM (no register spills) or 4
+   (registers capped at 128).
+   "phase_events" (0 or 1; default 0): renders record CUDA events on their
+   stream around each kernel for mk_render_phase_ms; not for renders that
+   are captured into a CUDA graph. */
 int mk_set_tuning(const char *name, int64_t value);
+
+/* Durations (ms) of the kernels of the last render launched with the
+   "phase_events" tuning set, on the current device: one for MK_FP64, three
+   (phases A, B, C) for the mixed forms; *nphases receives the count.
+   Waits for that render to finish.  No reference counterpart. */
+int mk_render_phase_ms(float *ms_out, int32_t *nphases);
 
 /* ------------------------------------------------------------ probes */
 /* FMA throughput probe (no reference counterpart): blocks x threads

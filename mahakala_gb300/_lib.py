@@ -18,13 +18,15 @@ _SZ = _c.c_size_t
 
 MK_OK, MK_ERR_ARG, MK_ERR_CUDA, MK_ERR_LIMIT, MK_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
 MK_RAY_ACTIVE, MK_RAY_CAPTURED, MK_RAY_ESCAPED, MK_RAY_MAXSTEPS, MK_RAY_NAN = 0, 1, 2, 3, 4
-MK_FP64, MK_MIXED, MK_MIXED_DF = 0, 1, 2
+MK_FP64, MK_MIXED, MK_MIXED_DF, MK_MIXED_STRICT = 0, 1, 2, 3
 MK_POLICY_REFERENCE, MK_POLICY_FIXED = 0, 1
 MK_CAMERA_GRID, MK_CAMERA_EQUATOR = 0, 1
 MK_MAX_NU = 4
 NOALLOC_WORKSPACE_BYTES = 16 << 20
 NOALLOC_MAX_MIXED_RAYS = (NOALLOC_WORKSPACE_BYTES - 256) // 320
 MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_TO_FP32, MK_WS_STEPS_FP64 = 1, 2, 3, 4, 6, 8
+MK_WS_SAMPLES_FP64 = 10
+MK_WS_ZONE_RUN_MAX = 11
 
 
 class MKError(RuntimeError):
@@ -91,6 +93,7 @@ SIGNATURES = {
     "mk_sizeof": (_SZ, [_c.c_char_p]),
     "mk_probe_fma": (_c.c_int, [_I32, _I32, _I32, _I64, _VP, _VP]),
     "mk_set_tuning": (_c.c_int, [_c.c_char_p, _I64]),
+    "mk_render_phase_ms": (_c.c_int, [_VP, _VP]),
 }
 
 _LIB = None

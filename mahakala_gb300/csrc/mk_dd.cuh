@@ -23,6 +23,7 @@ struct dd {
     float hi, lo;
     dd() = default;
     __host__ __device__ constexpr dd(float h, float l) : hi(h), lo(l) {}
+    __host__ __device__ explicit constexpr dd(float h) : hi(h), lo(0.0f) {}
     __host__ __device__ explicit constexpr dd(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
     __host__ __device__ double to_double() const { return (double)hi + (double)lo; }
 };
@@ -83,5 +84,6 @@ __host__ __device__ __forceinline__ double to_double(dd x) { return x.to_double(
 __host__ __device__ __forceinline__ double to_double(double x) { return x; }
 __host__ __device__ __forceinline__ float to_float(dd x) { return x.hi; }
 __host__ __device__ __forceinline__ float to_float(double x) { return (float)x; }
+__host__ __device__ __forceinline__ float to_float(float x) { return x; }
 
 }  // namespace mk

@@ -311,6 +311,25 @@ __device__ __forceinline__ bool locate_f32(const mk_snapshot_view &s, const Snap
     return true;
 }
 
+// Starts moving the 8 cells trilinear8_f32 will read for c into L1
+// (prefetch.global.L1 does not stall the issuing warp), so that the sample
+// taken after the next acceleration finds them there: the phases that run
+// one warp per sub-partition are latency-bound, not bandwidth-bound.  c comes
+// from a successful locate_f32, so every address lies in the block array.
+__device__ __forceinline__ void prefetch_cells_f32(const mk_snapshot_view &s, const CellPosF &c) {
+    const int n2 = s.n + 2;
+    const int64_t sj = (int64_t)n2 * 8, sk = (int64_t)n2 * n2 * 8;
+    const float *base = s.blocks + ((((int64_t)c.mb * n2 + c.idx[2]) * n2 + c.idx[1]) * n2 + c.idx[0]) * 8;
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            const float *p = base + dk * sk + dj * sj;
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 8));
+        }
+}
+
 __device__ __forceinline__ void trilinear8_f32(const mk_snapshot_view &s, const CellPosF &c, float prim[8]) {
     const int n2 = s.n + 2;
     const int64_t sj = (int64_t)n2 * 8, sk = (int64_t)n2 * n2 * 8;

@@ -47,6 +47,17 @@ constexpr double TWO_NINTHS = 0x1.c71c71c71c71cp-3;    // 2./9.
 constexpr double THIRD = 0x1.5555555555555p-2;         // 1./3
 constexpr double SIXTH = 0x1.5555555555555p-3;         // 1./6 (and 1/6 in RK4)
 
+// 1/6 in each arithmetic, built from literals so that no conversion from
+// double is left to run time (a run-time double -> pair split costs FP64
+// instructions in the pair code)
+template <typename T>
+__host__ __device__ constexpr T sixth() { return T(SIXTH); }
+template <>
+__host__ __device__ constexpr dd sixth<dd>() { return dd(0x1.555556p-3f, -0x1.555556p-28f); }
+
+// exact small constants in the arithmetic code are written as float
+// literals (0.5f, 2.0f, ...): the same value in double, float and pairs
+
 // Kerr-Schild metric data at a point: g = eta + f l l
 template <typename T>
 struct KerrPoint {
@@ -57,13 +68,13 @@ template <typename T>
 __device__ __forceinline__ KerrPoint<T> kerr_point(T x, T y, T z, T a) {
     const T aa = a * a;
     const T zz = z * z;
-    const T kk = T(0.5) * (x * x + y * y + zz - aa);
+    const T kk = T(0.5f) * (x * x + y * y + zz - aa);
     const T rr = sqrt(kk * kk + aa * zz) + kk;
     const T r = sqrt(rr);
     KerrPoint<T> m;
     m.r = r;
-    m.f = (T(2) * rr * r) / (rr * rr + aa * zz);
-    const T ira = T(1) / (rr + aa);
+    m.f = (T(2.0f) * rr * r) / (rr * rr + aa * zz);
+    const T ira = T(1.0f) / (rr + aa);
     m.l1 = (r * x + a * y) * ira;
     m.l2 = (r * y - a * x) * ira;
     m.l3 = z / r;
@@ -78,18 +89,18 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
                                            T &a3, KerrPoint<T> &m) {
     const T aa = a * a;
     const T zz = z * z;
-    const T kk = T(0.5) * (x * x + y * y + zz - aa);
+    const T kk = T(0.5f) * (x * x + y * y + zz - aa);
     const T Q = kk * kk + aa * zz;
     const T iq = inv_sqrt(Q);
     const T q = Q * iq;                      // sqrt(kk^2 + a^2 z^2)
     const T rr = q + kk;
     const T ir = inv_sqrt(rr);
     const T r = rr * ir;
-    const T i2rq = T(0.5) * ir * iq;         // 1 / (2 r q)
+    const T i2rq = T(0.5f) * ir * iq;         // 1 / (2 r q)
     const T den = rr * rr + aa * zz;
     const T rra = rr + aa;
     // one division for the two reciprocals 1/den and 1/(rr + a^2)
-    const T inv2 = T(1) / (den * rra);
+    const T inv2 = T(1.0f) / (den * rra);
     const T iden = rra * inv2;
     const T ira = den * inv2;
 
@@ -97,16 +108,16 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
     const T ry = rr * y * i2rq;
     const T rz = rra * z * i2rq;
 
-    const T f = T(2) * rr * r * iden;
-    const T c1 = T(3) * ir - T(4) * rr * r * iden;
+    const T f = T(2.0f) * rr * r * iden;
+    const T c1 = T(3.0f) * ir - T(4.0f) * rr * r * iden;
     const T fx = f * (c1 * rx);
     const T fy = f * (c1 * ry);
-    const T fz = f * (c1 * rz - T(2) * aa * z * iden);
+    const T fz = f * (c1 * rz - T(2.0f) * aa * z * iden);
 
     const T l1 = (r * x + a * y) * ira;
     const T l2 = (r * y - a * x) * ira;
     const T l3 = z * ir;
-    const T tr = T(2) * r;
+    const T tr = T(2.0f) * r;
     const T g1 = (x - tr * l1) * ira;
     const T g2 = (y - tr * l2) * ira;
     const T rira = r * ira, aira = a * ira;
@@ -127,7 +138,7 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
 
     const T Dflv = Df * lv;
     const T fDlv = f * Dlv;
-    const T half_lv2 = T(0.5) * lv * lv;
+    const T half_lv2 = T(0.5f) * lv * lv;
     const T flv = f * lv;
     const T F0 = -(Dflv + fDlv);
     const T F1 = -(Dflv * l1 + f * (Dl1 * lv) + l1 * fDlv) + fx * half_lv2 + flv * dlx;
@@ -161,25 +172,25 @@ __device__ __forceinline__ void rk4_step_k1(const T s[8], const T d1[4], T dt, T
     {
         const T k[8] = {dt * s[4], dt * s[5], dt * s[6], dt * s[7], dt * d1[0], dt * d1[1], dt * d1[2], dt * d1[3]};
 #pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = k[i]; tmp[i] = s[i] + T(0.5) * k[i]; }
+        for (int i = 0; i < 8; i++) { acc[i] = k[i]; tmp[i] = s[i] + T(0.5f) * k[i]; }
     }
     kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
     {
         const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
 #pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2) * k[i]; tmp[i] = s[i] + T(0.5) * k[i]; }
+        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2.0f) * k[i]; tmp[i] = s[i] + T(0.5f) * k[i]; }
     }
     kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
     {
         const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
 #pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2) * k[i]; tmp[i] = s[i] + k[i]; }
+        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2.0f) * k[i]; tmp[i] = s[i] + k[i]; }
     }
     kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
     {
         const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
 #pragma unroll
-        for (int i = 0; i < 8; i++) out[i] = s[i] + T(SIXTH) * (acc[i] + k[i]);
+        for (int i = 0; i < 8; i++) out[i] = s[i] + sixth<T>() * (acc[i] + k[i]);
     }
 }
 
@@ -264,6 +275,32 @@ __device__ __forceinline__ void rk4_step_pair(const f2 X[4], const f2 K[4], cons
     for (int i = 0; i < 4; i++) {
         Xo[i] = f2_add(X[i], f2_add(f2_mul(K[i], dt), c * (a1[i] + a2[i] + a3[i])));
         Ko[i] = f2_add(K[i], d * (a1[i] + 2.0f * a2[i] + 2.0f * a3[i] + a4[i]));
+    }
+}
+
+// The RK4 increments of one step in float, for a state held elsewhere in
+// higher precision: x, k the state rounded to float, a1 the acceleration
+// there.  dX = dt k + dt^2/6 (a1 + a2 + a3), dK = dt/6 (a1 + 2 a2 + 2 a3 + a4)
+// -- RK4_gen's combination (geodesics.py:317-336) written for x'' = a(x, x').
+__device__ __forceinline__ void rk4_increment_f32(const float x[4], const float k[4], const float a1[4], float dt,
+                                                  float a, float dX[4], float dK[4]) {
+    float t[8], a2[4], a3[4], a4[4];
+    const float h = 0.5f * dt;
+#pragma unroll
+    for (int i = 0; i < 4; i++) { t[i] = x[i] + h * k[i]; t[4 + i] = k[i] + h * a1[i]; }
+    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a2[0], a2[1], a2[2], a2[3]);
+#pragma unroll
+    for (int i = 0; i < 4; i++) { t[i] = x[i] + h * (k[i] + h * a1[i]); t[4 + i] = k[i] + h * a2[i]; }
+    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a3[0], a3[1], a3[2], a3[3]);
+#pragma unroll
+    for (int i = 0; i < 4; i++) { t[i] = x[i] + dt * (k[i] + h * a2[i]); t[4 + i] = k[i] + dt * a3[i]; }
+    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a4[0], a4[1], a4[2], a4[3]);
+    const float c = dt * dt * (1.0f / 6.0f);
+    const float d = dt * (1.0f / 6.0f);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        dX[i] = dt * k[i] + c * (a1[i] + a2[i] + a3[i]);
+        dK[i] = d * (a1[i] + 2.0f * a2[i] + 2.0f * a3[i] + a4[i]);
     }
 }
 

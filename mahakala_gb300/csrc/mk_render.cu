@@ -23,11 +23,15 @@
 //   MK_MIXED three launches on the caller's stream:
 //     A  FP32 from the camera.  A ray whose radius drops below R_FP64 (3 M),
 //        or that moves inward inside R_TURN (6 M, where photon-ring rays
-//        reach their turning points), is handed to an FP64 queue;
-//     B  FP64 over that queue: the near-horizon steps and the turning point.
-//        On entry the wavevector is renormalised to null in FP64.  A ray
-//        that leaves R_TURN outward is handed to an FP32 queue;
+//        reach their turning points), is handed to a queue (FP64 record);
+//     B  that queue, the near-horizon steps and the turning points, with
+//        the state in binary64 (render_zone_kernel): renormalised to null
+//        in binary64 on entry and at each radial turning point.  A ray
+//        that leaves R_TURN outward is handed to a second queue;
 //     C  FP32 over the second queue until the ray stops.
+//   MK_MIXED_STRICT: phase B integrates the geodesic entirely in binary64
+//   (render_fp64_kernel over the queue); MK_MIXED_DF: the same in
+//   double-float pairs.
 //   Splitting by precision keeps each warp uniform: on a part whose FP64
 //   rate is 1/64 of FP32, one FP64 lane would stall the other 31.  The
 //   intensity accumulates with a compensated (Kahan) FP32 sum and the
@@ -48,6 +52,36 @@ constexpr double R_TURN = 6.0;
 // "fp64_rays_per_warp"): 32 fills every lane; fewer rays per warp shorten
 // each warp's FP64 chain when the FP64 unit processes only active lanes
 static int g_fp64_rays_per_warp = 32;
+// 1: the mixed forms hand rays near the hole to FP64 (phase B); 0: phase A
+// keeps every ray in FP32 to its end (a measurement switch: it shows what
+// the FP64 region buys in accuracy)
+static int g_fp64_zone = 1;
+// resident blocks per SM the FP32 phases are compiled for: 3 (no register
+// spills) or 4 (registers capped at 128, a few spills)
+static int g_f32_blocks = 4;
+// measurement switch: when set, each render records a CUDA event on its
+// stream before its first kernel and after each kernel, so the phases can
+// be timed apart (mk_render_phase_ms).  Process-wide, off by default; not
+// for renders captured into a graph.
+static int g_phase_events = 0;
+static cudaEvent_t g_phase_ev[64][4];
+static bool g_phase_ev_made[64] = {false};
+static int g_phase_dev = -1, g_phase_n = 0;
+
+static int phase_mark(cudaStream_t st, int i) {
+    if (!g_phase_events) return MK_OK;
+    int dev = 0;
+    MK_CUDA(cudaGetDevice(&dev));
+    MK_REQUIRE(dev >= 0 && dev < 64, MK_ERR_LIMIT, "phase events: device ordinal %d not supported", dev);
+    if (!g_phase_ev_made[dev]) {
+        for (int k = 0; k < 4; k++) MK_CUDA(cudaEventCreate(&g_phase_ev[dev][k]));
+        g_phase_ev_made[dev] = true;
+    }
+    MK_CUDA(cudaEventRecord(g_phase_ev[dev][i], st));
+    g_phase_dev = dev;
+    g_phase_n = i;
+    return MK_OK;
+}
 
 // launch scratch: counters and work totals, then (mixed form) two queues
 struct RenderWorkspace {
@@ -61,6 +95,8 @@ struct RenderWorkspace {
     unsigned long long q32_next;
     unsigned long long steps_fp64;    // accepted steps taken in FP64 (mixed form)
     unsigned long long overflow;      // queue overflow (cannot happen: capacity = rays)
+    unsigned long long samples_fp64;  // in-snapshot samples taken in the FP64 phase (mixed form)
+    unsigned long long zone_run_max;  // most steps one ray took in one visit to the near-hole phase
 };
 constexpr size_t WS_HEADER = 256;
 static_assert(sizeof(RenderWorkspace) <= WS_HEADER, "workspace header");
@@ -180,37 +216,59 @@ __device__ __forceinline__ void renull_fp64(double s[8], double a) {
 }
 
 // ------------------------------------------------------------------ FP32
-// emission coefficients of one sample in float (mixed form): em, ab per
-// frequency (invariant, rescaled as in the FP64 path), and the step weight
-// w = -dt L.  Returns false outside the snapshot (no contribution).
-__device__ __forceinline__ bool emission_f32(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
-                                             const float s[8], const KerrPoint<float> &m,
-                                             const SynchroF32 sc[MK_MAX_NU], float em_out[MK_MAX_NU],
-                                             float ab_out[MK_MAX_NU]) {
-    CellPosF c;
-    if (!locate_f32(sv, sf, s[1], s[2], s[3], c)) return false;
+// A request's scalars in float, loaded once per ray: converting them from
+// the request's doubles at every sample would put ~12 instructions per step
+// on the FP64 pipe (1/64 rate), which the one-warp phases wait on.
+struct RayF32 {
+    float cos_fb, gam1, r_high, r_low, gem1, gim1, Ne_unit, B_unit, sigma_cut, L_unit, div, tol;
+    int nnu;
+};
+
+__device__ __forceinline__ RayF32 ray_f32(const mk_request &R) {
+    RayF32 c;
+    c.cos_fb = (float)R.cos_fallback_pitch;
+    c.gam1 = (float)(R.fluid_gamma - 1.);
+    c.r_high = (float)R.r_high;
+    c.r_low = (float)R.r_low;
+    c.gem1 = (float)R.electron_gamma_m1;
+    c.gim1 = (float)R.ion_gamma_m1;
+    c.Ne_unit = (float)R.Ne_unit;
+    c.B_unit = (float)R.B_unit;
+    c.sigma_cut = (float)R.sigma_cut;
+    c.L_unit = (float)R.L_unit;
+    c.div = (float)R.policy.div;
+    c.tol = (float)R.policy.tol;
+    c.nnu = R.nnu;
+    return c;
+}
+
+// emission coefficients of one sample in float (mixed forms) at the located
+// cell c: em, ab per frequency (invariant, rescaled as in the FP64 path)
+__device__ __forceinline__ void emission_f32_at(const mk_snapshot_view &sv, const CellPosF &c, const RayF32 &rc,
+                                                const float s[8], const KerrPoint<float> &m,
+                                                const SynchroF32 sc[MK_MAX_NU], float em_out[MK_MAX_NU],
+                                                float ab_out[MK_MAX_NU]) {
     float prim[8];
     trilinear8_f32(sv, c, prim);
-    const FluidF32 fs = fluid_frame_f32(prim, m, s + 4, (float)R.cos_fallback_pitch);
+    const FluidF32 fs = fluid_frame_f32(prim, m, s + 4, rc.cos_fb);
     const float bsq = fs.b * fs.b;
-    const float beta = fs.u * (float)(R.fluid_gamma - 1.) / bsq * 2.0f;
+    const float beta = fs.u * rc.gam1 / bsq * 2.0f;
     const float sigma = bsq / fs.dens;
     const float b2 = beta * beta;
-    const float T_ratio = ((float)R.r_high * b2 + (float)R.r_low) / (1.0f + b2);
-    const float gem1 = (float)R.electron_gamma_m1, gim1 = (float)R.ion_gamma_m1;
+    const float T_ratio = (rc.r_high * b2 + rc.r_low) / (1.0f + b2);
     // Theta_e = (MP/ME) u gem1 gim1 / (dens (gim1 + gem1 T_ratio))
-    const float Th = (float)(MP / ME) * fs.u * gem1 * gim1 / (fs.dens * (gim1 + gem1 * T_ratio));
-    const float Ne = (float)R.Ne_unit * fs.dens;
-    const float Bg = (float)R.B_unit * fs.b;
+    const float Th = (float)(MP / ME) * fs.u * rc.gem1 * rc.gim1 / (fs.dens * (rc.gim1 + rc.gem1 * T_ratio));
+    const float Ne = rc.Ne_unit * fs.dens;
+    const float Bg = rc.B_unit * fs.b;
     const float sin_p = sqrtf((1.0f - fs.cos_pitch) * (1.0f + fs.cos_pitch));
     const float th2 = Th * Th;
     // nus in Hz; nu' = -k.u (observed frequency rescaled to 1)
     const float nus = (float)(TWO_NINTHS * EE / TWO_PI_ME_CL) * Bg * th2 * sin_p;
     const float nup = -fs.kdotu;
-    const bool cut = sigma > (float)R.sigma_cut || Th < 0.3f;
+    const bool cut = sigma > rc.sigma_cut || Th < 0.3f;
 #pragma unroll
     for (int ch = 0; ch < MK_MAX_NU; ch++) {
-        if (ch < R.nnu) {
+        if (ch < rc.nnu) {
             const float nusp = nus * sc[ch].inv_nu;  // nus / nu_obs
             const float X = nup / nusp;
             const float x3 = cbrtf(X);
@@ -227,21 +285,21 @@ __device__ __forceinline__ bool emission_f32(const mk_request &R, const mk_snaps
             ab_out[ch] = isnan(ab) ? 0.0f : ab;
         }
     }
-    return true;
 }
 
-// one FP32 sample folded into a compensated (Kahan) float intensity sum
-__device__ __forceinline__ void sample_f32(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
+// one FP32 sample at the located cell folded into a compensated (Kahan)
+// float intensity sum; w = -dt L
+__device__ __forceinline__ void sample_f32(const mk_snapshot_view &sv, const CellPosF &c, const RayF32 &rc,
                                            const float s[8], const KerrPoint<float> &m, float dt_used,
                                            float I[MK_MAX_NU], float Ic[MK_MAX_NU], float P[MK_MAX_NU],
                                            const SynchroF32 sc[MK_MAX_NU], int &nsamples, float &max_tau) {
     float em[MK_MAX_NU], ab[MK_MAX_NU];
-    if (!emission_f32(R, sv, sf, s, m, sc, em, ab)) return;
+    emission_f32_at(sv, c, rc, s, m, sc, em, ab);
     ++nsamples;
-    const float w = -dt_used * (float)R.L_unit;
+    const float w = -dt_used * rc.L_unit;
 #pragma unroll
     for (int ch = 0; ch < MK_MAX_NU; ch++) {
-        if (ch < R.nnu) {
+        if (ch < rc.nnu) {
             const float tau = w * ab[ch];
             const float y = (w * em[ch]) * P[ch] - Ic[ch];
             const float t = I[ch] + y;
@@ -253,7 +311,26 @@ __device__ __forceinline__ void sample_f32(const mk_request &R, const mk_snapsho
     }
 }
 
-// FP32 emission at an FP64 or double-float state (mixed-form phase B),
+// FP32 emission at the located cell, accumulated in FP64 (near-hole phase)
+__device__ __forceinline__ void sample_f32_sum64(const mk_snapshot_view &sv, const CellPosF &c, const RayF32 &rc,
+                                                 const float s[8], const KerrPoint<float> &m, double w,
+                                                 double I[MK_MAX_NU], double P[MK_MAX_NU],
+                                                 const SynchroF32 sc[MK_MAX_NU], int &nsamples, double &max_tau) {
+    float em[MK_MAX_NU], ab[MK_MAX_NU];
+    emission_f32_at(sv, c, rc, s, m, sc, em, ab);
+    ++nsamples;
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++) {
+        if (ch < rc.nnu) {
+            const double tau = w * (double)ab[ch];
+            I[ch] += (w * (double)em[ch]) * P[ch];
+            P[ch] *= (1.0 - tau);
+            max_tau = fmax(max_tau, tau);
+        }
+    }
+}
+
+// FP32 emission at an FP64 or double-float state (strict and DF phase B),
 // accumulated in FP64
 template <typename T>
 __device__ __forceinline__ void sample_f32_at(const mk_request &R, const mk_snapshot_view &sv, const SnapF32 &sf,
@@ -269,19 +346,10 @@ __device__ __forceinline__ void sample_f32_at(const mk_request &R, const mk_snap
     m.l1 = to_float(m64.l1);
     m.l2 = to_float(m64.l2);
     m.l3 = to_float(m64.l3);
-    float em[MK_MAX_NU], ab[MK_MAX_NU];
-    if (!emission_f32(R, sv, sf, sf8, m, sc, em, ab)) return;
-    ++nsamples;
-    const double w = -dt_used * R.L_unit;
-#pragma unroll
-    for (int ch = 0; ch < MK_MAX_NU; ch++) {
-        if (ch < R.nnu) {
-            const double tau = w * (double)ab[ch];
-            I[ch] += (w * (double)em[ch]) * P[ch];
-            P[ch] *= (1.0 - tau);
-            max_tau = fmax(max_tau, tau);
-        }
-    }
+    CellPosF c;
+    if (!locate_f32(sv, sf, sf8[1], sf8[2], sf8[3], c)) return;
+    const RayF32 rc = ray_f32(R);
+    sample_f32_sum64(sv, c, rc, sf8, m, -dt_used * R.L_unit, I, P, sc, nsamples, max_tau);
 }
 
 enum { SRC_CAMERA = 0, SRC_QUEUE = 1 };
@@ -305,13 +373,14 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
     // lanes not on the stride never take work and stay masked off
     const bool lane_works = ((threadIdx.x & 31) % lane_stride) == 0;
     const long long total =
-        SRC == SRC_CAMERA ? total_camera : (long long)*(volatile unsigned long long *)&ws->q64_count;
+        SRC == SRC_CAMERA ? total_camera
+                          : min((long long)*(volatile unsigned long long *)&ws->q64_count, capacity);
     bool active = false, exhausted = false;
-    int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE, fp64_steps = 0;
+    int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE, fp64_steps = 0, fp64_samples = 0;
     long long ray = 0;
     int64_t pix = 0;
     T s[8], d1[4], dt = T(0.0);
-    double r_cur = 0.0, I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0;
+    double r_cur = 0.0, reh = 0.0, I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0;
     SynchroF32 sc[MK_MAX_NU];
     SnapF32 sf;
 
@@ -361,7 +430,8 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
             KerrPoint<T> m;
             kerr_accel(s[1], s[2], s[3], s[4], s[5], s[6], s[7], a, d1[0], d1[1], d1[2], d1[3], m);
             r_cur = to_double(m.r);
-            const double dt0 = reference_dt(r_cur, radius_eh(R.camera.bhspin), R.policy.div, R.policy.tol, why);
+            reh = radius_eh(R.camera.bhspin);
+            const double dt0 = reference_dt(r_cur, reh, R.policy.div, R.policy.tol, why);
             dt = T(dt0);
             if (dt0 == 0.0 || R.policy.nmax < 2) {
                 // stopped before its next step (reference K = steps), or N < 2
@@ -384,7 +454,7 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
             kerr_accel(nw[1], nw[2], nw[3], nw[4], nw[5], nw[6], nw[7], a, dn[0], dn[1], dn[2], dn[3], m);
             int w1;
             const double r_new = to_double(m.r);
-            const double dtn = reference_dt(r_new, radius_eh(R.camera.bhspin), R.policy.div, R.policy.tol, w1);
+            const double dtn = reference_dt(r_new, reh, R.policy.div, R.policy.tol, w1);
             if (dtn == 0.0) {
                 // the step is rejected and the ray stays frozen (geodesics.py:263-267)
                 finish_ray(R, pix, I, steps, w1, nsamples, max_tau, ws);
@@ -400,8 +470,11 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
                 ++fp64_steps;
                 if constexpr (SRC == SRC_CAMERA)
                     sample_fp64(R, snaps[R.snapshot], s, m, dt_used, I, P, nsamples, max_tau);
-                else  // mixed form: FP64 (or pair) geodesic, FP32 emission, FP64 sums
+                else {  // mixed form: FP64 (or pair) geodesic, FP32 emission, FP64 sums
+                    const int ns0 = nsamples;
                     sample_f32_at(R, snaps[R.snapshot], sf, s, m, dt_used, I, P, sc, nsamples, max_tau);
+                    fp64_samples += nsamples - ns0;
+                }
                 // trajectory rows stop at N-1: step N-1 never reaches the solve
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray(R, pix, I, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
@@ -430,6 +503,261 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
         }
     }
     if (SRC == SRC_QUEUE && fp64_steps) atomicAdd(&ws->steps_fp64, (unsigned long long)fp64_steps);
+    if (SRC == SRC_QUEUE && fp64_samples) atomicAdd(&ws->samples_fp64, (unsigned long long)fp64_samples);
+}
+
+// Mixed-form phase B (MK_MIXED): the rays near the hole.  The state is
+// held in binary64 and advanced by RK4 increments formed in float from the
+// state rounded to float (rk4_increment_f32); the wavevector is
+// renormalised to null in binary64 on entry and at every radial turning
+// point; the intensity and transmission sums are binary64.  The
+// accelerations and the emission are float, as in phases A and C: on this
+// part a binary64 acceleration costs ~33x a float one per step, and over
+// the measured images it changed the error against the FP64 form by less
+// than the float emission already contributes.  A ray leaving R_TURN
+// outward goes to the FP32 queue.
+//
+// Few rays reach this phase and its time is the serial chain of the
+// longest one, so each block runs two warps on two sub-partitions: warp 0
+// integrates 32 rays while warp 1 takes the samples of their previous step
+// (emission, sums, the image write), one step behind.  They exchange one
+// message per lane and step through a double buffer in shared memory and
+// meet at one named barrier per step (both warps execute it once per
+// iteration; the integrator's last message carries ZM_DONE and both leave
+// after that barrier).  No wait depends on another block.
+enum : unsigned { ZM_START = 1u, ZM_SAMPLE = 2u, ZM_END = 4u, ZM_PARK = 8u, ZM_DONE = 16u };
+constexpr int ZONE_THREADS = 64;
+
+struct ZoneMsgs {
+    unsigned flags[2][32];
+    int idx[2][32];   // ZM_START: index in the near-hole queue
+    int slot[2][32];  // ZM_PARK: slot in the second queue (a ray can start and park in one step)
+    int steps[2][32];
+    int why[2][32];
+    float s[2][8][32];  // state after the step
+    float m[2][5][32];  // r, f, l1, l2, l3 there
+    float dt[2][32];    // the step's size
+    int cmb[2][32];     // located cell (mb = -1: outside the snapshot)
+    int cidx[2][3][32];
+    float cdel[2][3][32];
+};
+
+__device__ __forceinline__ void zone_barrier() {
+    __syncwarp();  // the warp arrives converged
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+}
+
+__device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ reqs,
+                                               const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws,
+                                               RayRecord *q64, RayRecord *q32, long long capacity, ZoneMsgs &msg) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long *counter = &ws->q64_next;
+    const long long total = min((long long)*(volatile unsigned long long *)&ws->q64_count, capacity);
+    bool active = false, exhausted = false;
+    int rq = 0, steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0;
+    long long ray = 0;
+    double s[8], bhspin = 0.0;
+    float xf[8];  // s rounded to float
+    float d1[4], dt = 0.0f, r_cur = 0.0f, dr_prev = 0.0f, reh = 0.0f, a = 0.0f, div = 0.0f, tol = 0.0f;
+    SnapF32 sf;
+
+    for (int it = 0;; ++it) {
+        const int b = it & 1;
+        unsigned flags = 0;
+        const long long idx = fetch(!active && !exhausted, counter, total);
+        if (idx == -1) exhausted = true;
+        if (idx >= 0) {
+            const RayRecord &q = q64[idx];
+#pragma unroll
+            for (int i = 0; i < 8; i++) s[i] = q.s[i];
+            ray = q.ray;
+            steps = q.steps;
+            rq = q.rq;
+            const mk_request &R = reqs[rq];
+            bhspin = R.camera.bhspin;
+            nmax = R.policy.nmax;
+            div = (float)R.policy.div;
+            tol = (float)R.policy.tol;
+            renull_fp64(s, bhspin);
+            a = (float)bhspin;
+            reh = (float)radius_eh(bhspin);
+            sf = snap_f32(snaps[R.snapshot]);
+#pragma unroll
+            for (int i = 0; i < 8; i++) xf[i] = (float)s[i];
+            KerrPoint<float> m;
+            kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3], m);
+            r_cur = m.r;
+            dr_prev = 0.0f;
+            run = 0;
+            flags |= ZM_START;
+            msg.idx[b][lane] = (int)idx;
+            int why = MK_RAY_ACTIVE;
+            dt = reference_dt(r_cur, reh, div, tol, why);
+            if (dt == 0.0f || nmax < 2) {
+                flags |= ZM_END;
+                msg.why[b][lane] = why == MK_RAY_ACTIVE ? MK_RAY_MAXSTEPS : why;
+                msg.steps[b][lane] = steps;
+            } else {
+                active = true;
+            }
+        }
+        const bool any = __any_sync(0xffffffffu, active);
+        if (active) {
+            float dX[4], dK[4];
+            rk4_increment_f32(xf, xf + 4, d1, dt, a, dX, dK);
+            double sn[8];
+#pragma unroll
+            for (int i = 0; i < 4; i++) { sn[i] = s[i] + (double)dX[i]; sn[4 + i] = s[4 + i] + (double)dK[i]; }
+            float xn[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) xn[i] = (float)sn[i];
+            const mk_snapshot_view &sv = snaps[reqs[rq].snapshot];
+            CellPosF cell;
+            const bool inside = locate_f32(sv, sf, xn[1], xn[2], xn[3], cell);
+            if (inside) prefetch_cells_f32(sv, cell);
+            KerrPoint<float> m;
+            float dn[4];
+            kerr_accel(xn[1], xn[2], xn[3], xn[4], xn[5], xn[6], xn[7], a, dn[0], dn[1], dn[2], dn[3], m);
+            int w1;
+            const float r_new = m.r;
+            const float dtn = reference_dt(r_new, reh, div, tol, w1);
+            if (dtn == 0.0f) {
+                // the step is rejected and the ray stays frozen (geodesics.py:263-267)
+                flags |= ZM_END;
+                msg.why[b][lane] = w1;
+                msg.steps[b][lane] = steps;
+                active = false;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; i++) { s[i] = sn[i]; xf[i] = xn[i]; }
+#pragma unroll
+                for (int i = 0; i < 4; i++) d1[i] = dn[i];
+                flags |= ZM_SAMPLE;
+#pragma unroll
+                for (int i = 0; i < 8; i++) msg.s[b][i][lane] = xn[i];
+                msg.m[b][0][lane] = m.r;
+                msg.m[b][1][lane] = m.f;
+                msg.m[b][2][lane] = m.l1;
+                msg.m[b][3][lane] = m.l2;
+                msg.m[b][4][lane] = m.l3;
+                msg.dt[b][lane] = dt;
+                msg.cmb[b][lane] = inside ? cell.mb : -1;
+#pragma unroll
+                for (int i = 0; i < 3; i++) { msg.cidx[b][i][lane] = cell.idx[i]; msg.cdel[b][i][lane] = cell.del[i]; }
+                dt = dtn;
+                ++steps;
+                ++zone_steps;
+                run_max = max(run_max, ++run);
+                const float dr = r_new - r_cur;
+                if (steps >= nmax - 1) {
+                    // trajectory rows stop at N-1: step N-1 never reaches the solve
+                    flags |= ZM_END;
+                    msg.why[b][lane] = MK_RAY_MAXSTEPS;
+                    msg.steps[b][lane] = steps;
+                    active = false;
+                } else if (r_new >= (float)R_TURN && dr > 0.0f) {
+                    // outbound past the photon-ring region: back to FP32
+                    const unsigned long long slot = atomicAdd(&ws->q32_count, 1ull);
+                    if ((long long)slot < capacity) {
+                        RayRecord &q = q32[slot];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) q.s[i] = s[i];
+                        q.ray = ray;
+                        q.steps = steps;
+                        q.rq = rq;
+                        flags |= ZM_PARK;
+                        msg.slot[b][lane] = (int)slot;
+                        active = false;
+                    } else {
+                        atomicAdd(&ws->overflow, 1ull);  // keep integrating here
+                    }
+                } else if ((dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f)) {
+                    // radial turning point: renormalise to null in binary64 and
+                    // re-evaluate the first stage of the next step there
+                    renull_fp64(s, bhspin);
+                    xf[4] = (float)s[4];
+                    kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3]);
+                }
+                r_cur = r_new;
+                dr_prev = dr;
+            }
+        }
+        msg.flags[b][lane] = flags | (any ? 0u : ZM_DONE);
+        zone_barrier();
+        if (!any) break;
+    }
+    if (zone_steps) atomicAdd(&ws->steps_fp64, (unsigned long long)zone_steps);
+    if (run_max) atomicMax(&ws->zone_run_max, (unsigned long long)run_max);
+}
+
+__device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
+                                            const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws,
+                                            const RayRecord *q64, RayRecord *q32, const ZoneMsgs &msg) {
+    const int lane = threadIdx.x & 31;
+    int rq = 0, nsamples = 0, zone_samples = 0;
+    int64_t pix = 0;
+    double I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0, L_unit = 0.0;
+    SynchroF32 sc[MK_MAX_NU];
+    RayF32 rc;
+    for (int it = 0;; ++it) {
+        const int b = it & 1;
+        zone_barrier();
+        const unsigned flags = msg.flags[b][lane];
+        if (flags & ZM_START) {
+            const RayRecord &q = q64[msg.idx[b][lane]];
+#pragma unroll
+            for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = q.I[ch]; P[ch] = q.P[ch]; }
+            max_tau = q.max_tau;
+            nsamples = q.nsamples;
+            rq = q.rq;
+            const mk_request &R = reqs[rq];
+            pix = q.ray - R.ray_offset;
+            L_unit = R.L_unit;
+            rc = ray_f32(R);
+#pragma unroll
+            for (int ch = 0; ch < MK_MAX_NU; ch++)
+                if (ch < R.nnu) sc[ch] = synchro_consts(R.nu[ch]);
+        }
+        if ((flags & ZM_SAMPLE) && msg.cmb[b][lane] >= 0) {
+            CellPosF c;
+            c.mb = msg.cmb[b][lane];
+#pragma unroll
+            for (int i = 0; i < 3; i++) { c.idx[i] = msg.cidx[b][i][lane]; c.del[i] = msg.cdel[b][i][lane]; }
+            float x[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) x[i] = msg.s[b][i][lane];
+            KerrPoint<float> m;
+            m.r = msg.m[b][0][lane];
+            m.f = msg.m[b][1][lane];
+            m.l1 = msg.m[b][2][lane];
+            m.l2 = msg.m[b][3][lane];
+            m.l3 = msg.m[b][4][lane];
+            sample_f32_sum64(snaps[reqs[rq].snapshot], c, rc, x, m, -(double)msg.dt[b][lane] * L_unit, I, P, sc,
+                             nsamples, max_tau);
+            ++zone_samples;
+        }
+        if (flags & ZM_END) {
+            finish_ray(reqs[rq], pix, I, msg.steps[b][lane], msg.why[b][lane], nsamples, max_tau, ws);
+        } else if (flags & ZM_PARK) {
+            RayRecord &q = q32[msg.slot[b][lane]];
+#pragma unroll
+            for (int ch = 0; ch < MK_MAX_NU; ch++) { q.I[ch] = I[ch]; q.P[ch] = P[ch]; }
+            q.max_tau = max_tau;
+            q.nsamples = nsamples;
+        }
+        if (flags & ZM_DONE) break;
+    }
+    if (zone_samples) atomicAdd(&ws->samples_fp64, (unsigned long long)zone_samples);
+}
+
+__global__ void __launch_bounds__(ZONE_THREADS)
+render_zone_kernel(const mk_request *__restrict__ reqs, const mk_snapshot_view *__restrict__ snaps,
+                   RenderWorkspace *ws, RayRecord *q64, RayRecord *q32, long long capacity) {
+    __shared__ ZoneMsgs msg;
+    if (threadIdx.x < 32)
+        zone_integrate(reqs, snaps, ws, q64, q32, capacity, msg);
+    else
+        zone_sample(reqs, snaps, ws, q64, q32, msg);
 }
 
 __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix, const float I[MK_MAX_NU],
@@ -445,18 +773,19 @@ __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix,
 // hand-off to the FP64 queue.  SRC_QUEUE: phase C over the FP32 queue.
 // The ray state is a float pair per component (rk4_step_pair); the
 // accelerations, the sampling and the emission are plain float.
-template <int SRC>
-__global__ void __launch_bounds__(RENDER_THREADS)
+template <int SRC, int MINB>
+__global__ void __launch_bounds__(RENDER_THREADS, MINB)
 render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
                   const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64, RayRecord *q32,
-                  long long capacity, const mk_job *job) {
+                  long long capacity, const mk_job *job, int zone) {
     if (job) {
         nreq = job->nreq;
         total_camera = job->total_rays;
     }
     unsigned long long *counter = SRC == SRC_CAMERA ? &ws->counter : &ws->q32_next;
     const long long total =
-        SRC == SRC_CAMERA ? total_camera : (long long)*(volatile unsigned long long *)&ws->q32_count;
+        SRC == SRC_CAMERA ? total_camera
+                          : min((long long)*(volatile unsigned long long *)&ws->q32_count, capacity);
     bool active = false, exhausted = false;
     int rq = 0, steps = 0, nsamples = 0, why = MK_RAY_ACTIVE;
     long long ray = 0;
@@ -466,6 +795,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
     float I[MK_MAX_NU], Ic[MK_MAX_NU], P[MK_MAX_NU];
     SynchroF32 sc[MK_MAX_NU];
     SnapF32 sf;
+    RayF32 rc;
 
     for (;;) {
         const long long idx = fetch(!active && !exhausted, counter, total);
@@ -508,11 +838,12 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
             for (int ch = 0; ch < MK_MAX_NU; ch++)
                 if (ch < R.nnu) sc[ch] = synchro_consts(R.nu[ch]);
             sf = snap_f32(snaps[R.snapshot]);
+            rc = ray_f32(R);
             KerrPoint<float> m;
             kerr_accel(X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi, a, d1[0], d1[1], d1[2], d1[3],
                        m);
             r_cur = m.r;
-            dt = reference_dt(r_cur, reh, (float)R.policy.div, (float)R.policy.tol, why);
+            dt = reference_dt(r_cur, reh, rc.div, rc.tol, why);
             if (dt == 0.0f || R.policy.nmax < 2) {
                 if (why == MK_RAY_ACTIVE) why = MK_RAY_MAXSTEPS;
                 finish_ray_f32(R, pix, I, Ic, steps, why, nsamples, max_tau, ws);
@@ -526,12 +857,16 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
             f2 Xn[4], Kn[4];
             float dn[4];
             rk4_step_pair(X, K, d1, dt, a, Xn, Kn);
+            const mk_snapshot_view &sv = snaps[R.snapshot];
+            CellPosF cell;
+            const bool inside = locate_f32(sv, sf, Xn[1].hi, Xn[2].hi, Xn[3].hi, cell);
+            if (inside) prefetch_cells_f32(sv, cell);
             KerrPoint<float> m;
             kerr_accel(Xn[1].hi, Xn[2].hi, Xn[3].hi, Kn[0].hi, Kn[1].hi, Kn[2].hi, Kn[3].hi, a, dn[0], dn[1], dn[2],
                        dn[3], m);
             int w1;
             const float r_new = m.r;
-            const float dtn = reference_dt(r_new, reh, (float)R.policy.div, (float)R.policy.tol, w1);
+            const float dtn = reference_dt(r_new, reh, rc.div, rc.tol, w1);
             if (dtn == 0.0f) {
                 finish_ray_f32(R, pix, I, Ic, steps, w1, nsamples, max_tau, ws);
                 active = false;
@@ -542,11 +877,11 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 dt = dtn;
                 ++steps;
                 const float sh[8] = {X[0].hi, X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi};
-                sample_f32(R, snaps[R.snapshot], sf, sh, m, dt_used, I, Ic, P, sc, nsamples, max_tau);
+                if (inside) sample_f32(sv, cell, rc, sh, m, dt_used, I, Ic, P, sc, nsamples, max_tau);
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
                     active = false;
-                } else if (SRC == SRC_CAMERA &&
+                } else if (SRC == SRC_CAMERA && zone &&
                            (r_new < (float)R_FP64 || (r_new < (float)R_TURN && r_new < r_cur))) {
                     // near the horizon or inbound in the photon-ring region: FP64
                     const unsigned long long slot = atomicAdd(&ws->q64_count, 1ull);
@@ -577,7 +912,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
 
 template <typename K>
 static int blocks_per_sm(K kernel, int slot) {
-    static int cached[64][4] = {{0}};
+    static int cached[64][8] = {{0}};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 64 && cached[dev][slot]) return cached[dev][slot];
@@ -606,12 +941,27 @@ extern "C" int mk_set_tuning(const char *name, int64_t value) {
         g_fp64_rays_per_warp = (int)value;
         return MK_OK;
     }
+    if (!strcmp(name, "f32_blocks_per_sm")) {
+        MK_REQUIRE(value == 3 || value == 4, MK_ERR_ARG, "mk_set_tuning: f32_blocks_per_sm must be 3 or 4");
+        g_f32_blocks = (int)value;
+        return MK_OK;
+    }
+    if (!strcmp(name, "phase_events")) {
+        MK_REQUIRE(value == 0 || value == 1, MK_ERR_ARG, "mk_set_tuning: phase_events must be 0 or 1");
+        g_phase_events = (int)value;
+        return MK_OK;
+    }
+    if (!strcmp(name, "fp64_zone")) {
+        MK_REQUIRE(value == 0 || value == 1, MK_ERR_ARG, "mk_set_tuning: fp64_zone must be 0 or 1");
+        g_fp64_zone = (int)value;
+        return MK_OK;
+    }
     MK_REQUIRE(false, MK_ERR_ARG, "mk_set_tuning: unknown parameter '%s'", name);
 }
 
 extern "C" size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision) {
     if (total_rays < 0) return 0;
-    if (precision == MK_MIXED || precision == MK_MIXED_DF)
+    if (precision == MK_MIXED || precision == MK_MIXED_DF || precision == MK_MIXED_STRICT)
         return WS_HEADER + 2 * (size_t)total_rays * sizeof(RayRecord);
     return WS_HEADER;
 }
@@ -622,43 +972,61 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     MK_CUDA(cudaMemsetAsync(workspace_dev, 0, WS_HEADER, st));
     if (max_rays == 0) return MK_OK;
     RenderWorkspace *ws = (RenderWorkspace *)workspace_dev;
+    int rc = phase_mark(st, 0);
+    if (rc != MK_OK) return rc;
     if (precision == MK_FP64) {
         const unsigned grid = persistent_grid(blocks_per_sm(render_fp64_kernel<SRC_CAMERA>, 0), max_rays);
         render_fp64_kernel<SRC_CAMERA><<<grid, RENDER_THREADS, 0, st>>>(reqs_dev, nreq, (long long)total_rays,
                                                                         snaps_dev, ws, nullptr, nullptr, 0, 1,
                                                                         job_dev);
         MK_LAUNCHED("render_fp64_kernel");
-        return MK_OK;
+        return phase_mark(st, 1);
     }
     RayRecord *q64 = (RayRecord *)((char *)workspace_dev + WS_HEADER);
     RayRecord *q32 = q64 + max_rays;
     const long long cap = (long long)max_rays;
-    render_f32_kernel<SRC_CAMERA>
-        <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA>, 1), max_rays), RENDER_THREADS, 0, st>>>(
-            reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev);
+    if (g_f32_blocks == 4)
+        render_f32_kernel<SRC_CAMERA, 4>
+            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 4>, 1), max_rays), RENDER_THREADS, 0,
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, g_fp64_zone);
+    else
+        render_f32_kernel<SRC_CAMERA, 3>
+            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 3>, 2), max_rays), RENDER_THREADS, 0,
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, g_fp64_zone);
     MK_LAUNCHED("render_f32_kernel (camera)");
+    if ((rc = phase_mark(st, 1)) != MK_OK) return rc;
     // The queues' sizes are only known on the device: persistent grids.
     // Phase B runs one warp per block, 4 blocks per SM: the few FP64 rays
     // spread over every SM sub-partition instead of queuing on the FP64
     // units of a few SMs (one FP64 warp instruction occupies a
     // sub-partition's FP64 unit for tens of cycles on this part).
-    {
+    if (precision == MK_MIXED) {
+        render_zone_kernel<<<(unsigned)device_sm_count() * 4, ZONE_THREADS, 0, st>>>(reqs_dev, snaps_dev, ws, q64,
+                                                                                      q32, cap);
+        MK_LAUNCHED("render_zone_kernel");
+    } else {
         const int per_warp = g_fp64_rays_per_warp;
         const int stride = 32 / per_warp;
         const unsigned grid = (unsigned)device_sm_count() * (per_warp >= 32 ? 4 : 16);
-        if (precision == MK_MIXED)
+        if (precision == MK_MIXED_STRICT)
             render_fp64_kernel<SRC_QUEUE, double>
                 <<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, stride, job_dev);
         else
             render_fp64_kernel<SRC_QUEUE, dd>
                 <<<grid, 32, 0, st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, stride, job_dev);
+        MK_LAUNCHED("render_fp64_kernel (queue)");
     }
-    MK_LAUNCHED("render_fp64_kernel (queue)");
-    render_f32_kernel<SRC_QUEUE>
-        <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE>, 3), max_rays), RENDER_THREADS, 0, st>>>(
-            reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev);
+    if ((rc = phase_mark(st, 2)) != MK_OK) return rc;
+    if (g_f32_blocks == 4)
+        render_f32_kernel<SRC_QUEUE, 4>
+            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 4>, 3), max_rays), RENDER_THREADS, 0,
+               st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
+    else
+        render_f32_kernel<SRC_QUEUE, 3>
+            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 3>, 4), max_rays), RENDER_THREADS, 0,
+               st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
     MK_LAUNCHED("render_f32_kernel (queue)");
-    return MK_OK;
+    return phase_mark(st, 3);
 }
 
 }  // namespace mk
@@ -668,8 +1036,8 @@ extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
                          void *workspace_dev, size_t workspace_bytes, void *stream) {
     MK_REQUIRE(reqs_dev && snaps_dev && workspace_dev, MK_ERR_ARG, "mk_render: null pointer");
     MK_REQUIRE(nreq > 0 && nsnap > 0 && total_rays >= 0, MK_ERR_ARG, "mk_render: bad sizes");
-    MK_REQUIRE(precision == MK_FP64 || precision == MK_MIXED || precision == MK_MIXED_DF, MK_ERR_ARG,
-               "mk_render: unknown precision %d", (int)precision);
+    MK_REQUIRE(precision >= MK_FP64 && precision <= MK_MIXED_STRICT, MK_ERR_ARG, "mk_render: unknown precision %d",
+               (int)precision);
     const size_t need = mk_render_workspace_bytes(total_rays, precision);
     MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render: workspace of %zu bytes, need %zu",
                workspace_bytes, need);
@@ -683,7 +1051,7 @@ extern "C" int mk_render_job(const mk_job *job_dev, const mk_request *reqs_dev, 
                              void *stream) {
     MK_REQUIRE(job_dev && reqs_dev && snaps_dev && workspace_dev, MK_ERR_ARG, "mk_render_job: null pointer");
     MK_REQUIRE(max_rays >= 0, MK_ERR_ARG, "mk_render_job: negative max_rays");
-    MK_REQUIRE(precision == MK_FP64 || precision == MK_MIXED || precision == MK_MIXED_DF, MK_ERR_ARG,
+    MK_REQUIRE(precision >= MK_FP64 && precision <= MK_MIXED_STRICT, MK_ERR_ARG,
                "mk_render_job: unknown precision %d", (int)precision);
     const size_t need = mk_render_workspace_bytes(max_rays, precision);
     MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render_job: workspace of %zu bytes, need %zu",
@@ -695,3 +1063,18 @@ extern "C" int mk_render_job(const mk_job *job_dev, const mk_request *reqs_dev, 
 
 // the allocation-free entry point sizes its static workspace from these
 static_assert(mk::WS_HEADER == 256 && sizeof(mk::RayRecord) == 160, "MK_NOALLOC_MAX_MIXED_RAYS assumes 256 + 320 B/ray");
+
+extern "C" int mk_render_phase_ms(float *ms_out, int32_t *nphases) {
+    MK_REQUIRE(ms_out && nphases, MK_ERR_ARG, "mk_render_phase_ms: null pointer");
+    MK_REQUIRE(mk::g_phase_dev >= 0 && mk::g_phase_n > 0, MK_ERR_ARG,
+               "mk_render_phase_ms: no render recorded its phases (set the phase_events tuning first)");
+    int cur = 0;
+    MK_CUDA(cudaGetDevice(&cur));
+    MK_REQUIRE(cur == mk::g_phase_dev, MK_ERR_ARG, "mk_render_phase_ms: the last render ran on device %d",
+               mk::g_phase_dev);
+    cudaEvent_t *ev = mk::g_phase_ev[mk::g_phase_dev];
+    MK_CUDA(cudaEventSynchronize(ev[mk::g_phase_n]));
+    for (int i = 0; i < mk::g_phase_n; i++) MK_CUDA(cudaEventElapsedTime(&ms_out[i], ev[i], ev[i + 1]));
+    *nphases = mk::g_phase_n;
+    return MK_OK;
+}

@@ -21,7 +21,8 @@ from .geodesics import camera_pixels, make_camera, step_policy
 
 __all__ = ["make_image", "RenderRequest", "PreparedRender", "render_requests", "image_flux_jy"]
 
-PRECISIONS = {"fp64": _lib.MK_FP64, "mixed": _lib.MK_MIXED, "mixed_df": _lib.MK_MIXED_DF}
+PRECISIONS = {"fp64": _lib.MK_FP64, "mixed": _lib.MK_MIXED, "mixed_df": _lib.MK_MIXED_DF,
+              "mixed_strict": _lib.MK_MIXED_STRICT}
 
 
 @dataclass
@@ -135,6 +136,17 @@ class PreparedRender:
         FP64) of the last mixed-form launch (syncs)."""
         w = self.ws[:32].cpu()
         return int(w[_lib.MK_WS_TO_FP64]), int(w[_lib.MK_WS_TO_FP32]), int(w[_lib.MK_WS_STEPS_FP64])
+
+    def samples_fp64(self):
+        """In-snapshot samples taken in the FP64 phase of the last
+        mixed-form launch (syncs)."""
+        return int(self.ws[:32].cpu()[_lib.MK_WS_SAMPLES_FP64])
+
+    def zone_run_max(self):
+        """Most steps one ray took in one visit to the mixed form's
+        near-hole phase in the last launch (syncs): that phase's serial
+        chain."""
+        return int(self.ws[:32].cpu()[_lib.MK_WS_ZONE_RUN_MAX])
 
     def max_step_optical_depth(self):
         """Largest per-step w*alpha of the last launch (syncs); the explicit

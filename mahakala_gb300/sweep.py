@@ -63,7 +63,7 @@ def run(resolution=512, precision="mixed", spins=None, inclinations=None, r_high
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--resolution", type=int, default=512)
-    p.add_argument("--precision", default="mixed", choices=["mixed", "mixed_df"])
+    p.add_argument("--precision", default="mixed", choices=["mixed", "mixed_strict", "mixed_df"])
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
     t0 = time.time()

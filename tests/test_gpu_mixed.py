@@ -1,5 +1,8 @@
-"""Mixed-precision render (FP32 with FP64 near the hole and at the photon
-ring) against the FP64 render of the same request.
+"""Mixed-precision renders against the FP64 render of the same request:
+``mixed`` (FP32 arithmetic, binary64 ray state, sums and null
+renormalisation near the hole and at the photon-ring turning points),
+``mixed_strict`` (the whole near-hole geodesic step in binary64) and
+``mixed_df`` (that step in double-float pairs).
 
 Bar: total-flux relative error <= 1e-3 and max per-pixel relative error
 <= 1e-2 (floor 1e-4 of the image maximum), captured masks (shadow) equal
@@ -32,7 +35,7 @@ def _pair(model, precision, **kw):
     return i64, imx, r64.out["status"].cpu().numpy(), rmx.out["status"].cpu().numpy()
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_strict", "mixed_df"])
 @pytest.mark.parametrize("spin,inc,rh", [(0.94, 17.0, 40.0), (0.5, 60.0, 10.0), (0.0, 85.0, 1.0)])
 def test_mixed_matches_fp64(cuda, medium_model, precision, spin, inc, rh):
     from mahakala_gb300 import configs, metrics
@@ -47,7 +50,7 @@ def test_mixed_matches_fp64(cuda, medium_model, precision, spin, inc, rh):
     assert abs(m["shadow_diameter"] - m["shadow_diameter_fp64"]) <= 2 * 50.0 / 48
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_strict", "mixed_df"])
 def test_mixed_multifrequency_and_batch(cuda, medium_model, precision):
     """Three frequencies in one mixed pass, and a batch of requests, each
     within the bar of its FP64 render."""
@@ -68,10 +71,10 @@ def test_mixed_multifrequency_and_batch(cuda, medium_model, precision):
             assert metrics.max_pixel_rel_err(imx[c], i64[c]) <= PIX_TOL
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_strict", "mixed_df"])
 def test_mixed_hands_rays_to_fp64(cuda, medium_model, precision):
-    """Captured rays and photon-ring rays are integrated in FP64 (or pairs)
-    near the hole."""
+    """Captured rays and photon-ring rays leave the FP32 phase near the hole
+    and come back when they leave it outward."""
     from mahakala_gb300.images import PreparedRender, RenderRequest
     prep = PreparedRender([RenderRequest(medium_model, camera_inclination=17.0, resolution=32, fov=50.0,
                                          max_nsteps=8192)], precision=precision)

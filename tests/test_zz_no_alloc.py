@@ -22,7 +22,7 @@ def _model(arrs):
     return AthenakFluidModel(arrs, arrs.bhspin, fluid_gamma=13. / 9)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_strict"])
 def test_noalloc_matches_workspace_render(cuda, tiny_arrays, precision):
     import torch
 
