@@ -46,6 +46,11 @@ FLOP_PER_EXTRA_NU = 41
 
 L2_FLUSH_BYTES = 256 << 20
 
+# FP64 FLOP (DFMA = 2) per point of the standalone sampling stage, from ncu's
+# DADD/DMUL/DFMA thread-instruction counters on fluid_scalars_kernel (64x64
+# camera over the 256^3-cell snapshot, 19 % of points inside it)
+SAMPLING_FP64_FLOP_PER_POINT = 399
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -61,6 +66,9 @@ def parse():
     p.add_argument("--resolution", type=int, default=0, help="override the image size (profiling small cases)")
     p.add_argument("--serving", type=int, default=60,
                    help="requests in the served Poisson stream (0 = skip the serving measurement)")
+    p.add_argument("--sampling-rays", type=int, default=-1,
+                   help="rays per side of the standalone sampling-stage measurement (0 = skip; default 128 for "
+                        "stress1024, 0 otherwise)")
     p.add_argument("--quick", action="store_true",
                    help="device timing only: skip the FMA probes, the end-to-end pass and the CPU baseline")
     return p.parse_args()
@@ -328,7 +336,7 @@ def hbm_peak():
         return 6800.0, "fallback (6.8 TB/s, one earlier GB300 copy measurement)"
 
 
-def sampling_stage(torch, model, spec, flush, stream, rays_per_side=128, reps=3):
+def sampling_stage(torch, model, spec, flush, stream, fp64_peak, rays_per_side=128, reps=3):
     """The sampling stage alone (get_fluid_scalars_from_geodesics as the
     standalone mk_fluid_scalars kernel) over the reference's trajectory rows
     of a rays_per_side^2 camera with the workload's view: every row of every
@@ -370,15 +378,21 @@ def sampling_stage(torch, model, spec, flush, stream, rays_per_side=128, reps=3)
         ts.append(e0.elapsed_time(e1) * 1e-3)
     t = statistics.mean(ts)
     nbytes = n * (64 + 40) + inside * 256
+    flops = SAMPLING_FP64_FLOP_PER_POINT * n
     peak, src = hbm_peak()
     del S, pts, out
     torch.cuda.empty_cache()
-    return {"kernel": "fluid_scalars_kernel", "bound": "hbm", "rays": rays_per_side ** 2, "rows": nt,
+    return {"kernel": "fluid_scalars_kernel", "bound": "fp64", "rays": rays_per_side ** 2, "rows": nt,
             "points": n, "in_snapshot": inside, "ms": 1e3 * t, "algorithmic_bytes": nbytes,
-            "achieved": nbytes / t / 1e9, "peak": peak, "unit": "GB/s", "frac": nbytes / t / 1e9 / peak,
-            "peak_source": src, "traffic": None,
-            "note": "algorithmic bytes assume every gather from DRAM; neighbouring samples of a ray share "
-                    "cells, so L2 serves part of them (DRAM traffic from ncu in profiles/)"}
+            "hbm": {"achieved": nbytes / t / 1e9, "peak": peak, "unit": "GB/s", "frac": nbytes / t / 1e9 / peak,
+                    "peak_source": src},
+            "fp64": {"achieved": flops / t / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": flops / t / fp64_peak, "flop_per_point": SAMPLING_FP64_FLOP_PER_POINT},
+            "traffic": None,
+            "note": "every point needs the metric, fluid frame and arccos in binary64 to return the reference's "
+                    "values, so the stage is FP64-pipe bound (ncu: 87.5 % FP64 pipe, 2.6 % DRAM; "
+                    "profiles/fluid_scalars_kernel_sampling64.md); FLOP per point from ncu's FP64 instruction "
+                    "counters on the 64x64 case"}
 
 
 def run_vacuum(args):
@@ -529,8 +543,10 @@ def main():
     clocks = clocks_summary(proc, fh, cpath, local) if rank == 0 else None
 
     sampling = None
-    if args.workload == "stress1024" and not args.quick:
-        sampling = sampling_stage(torch, model, spec, flush, stream)
+    srays = args.sampling_rays if args.sampling_rays >= 0 else (128 if args.workload == "stress1024" else 0)
+    if srays:
+        sampling = sampling_stage(torch, model, spec, flush, stream, peak64 if not args.quick else float("nan"),
+                                  rays_per_side=srays)
 
     serving = None
     if args.serving and not args.quick and args.workload == "render256":
@@ -565,9 +581,12 @@ def main():
             # phase A does the FP32 steps up to the hand-off, phase C the rest;
             # their split is not counted, so both carry the FP32 total over their sum
             tA, tB, tC = r["t_phase"]
-            kernels = [("render_f32_kernel (phases A+C)", "fp32", f32, tA + tC, peak32),
-                       ("render_fp64_kernel (phase B, FP64 queue)", "fp64",
-                        steps64 * FLOP_PER_STEP + r["samples64"] * per_sample, tB, peak64)]
+            zone = steps64 * FLOP_PER_STEP + r["samples64"] * per_sample
+            if form == "mixed":  # float accelerations and emission, binary64 state and sums
+                kb = ("render_zone_kernel (phase B, near the hole)", "fp32", zone, tB, peak32)
+            else:
+                kb = ("render_fp64_kernel (phase B, near the hole)", "fp64", zone, tB, peak64)
+            kernels = [("render_f32_kernel (phases A+C)", "fp32", f32, tA + tC, peak32), kb]
         table = [{"kernel": k, "bound": b, "flop": fl, "ms": 1e3 * t, "achieved": fl / t / 1e12 if t else None,
                   "peak": pk / 1e12, "frac": fl / t / pk if t else None} for k, b, fl, t, pk in kernels]
         top = max(table, key=lambda e: e["ms"])
@@ -579,8 +598,8 @@ def main():
             out["traffic_note"] = ("ncu on the 192x192 case: 242 MB DRAM read per launch; the kernel is "
                                    "FP64-pipe bound (profiles/render_fp64_kernel_render192.md)")
         else:
-            out["note"] = ("phase B is bound by the serial chain of the longest FP64 ray (one FP64 warp "
-                           "instruction per sub-partition at a time), not by FP64 throughput")
+            out["note"] = ("phase B runs the serial chain of its longest ray (zone_run_max steps) on one warp "
+                           "per sub-partition: latency-bound, not throughput-bound")
         return out
 
     def form_line(form):

@@ -114,6 +114,16 @@ typedef struct {
     int32_t *nsteps;                         /* (npx) device output or NULL */
     int32_t *status;                         /* (npx) device output or NULL */
     int64_t ray_offset;                      /* first global ray of this request */
+    /* Per-step diagnostics, MK_FP64 only (NULL to skip): for trajectory row
+       i (1 <= i < rows) of each ray, rows_em/rows_ab (nnu, rows, npx)
+       receive the invariant emissivity and absorptivity of the sample
+       there (after the sigma cut; 0 outside the snapshot) and rows_dt
+       (rows, npx) the step size dt of row i-1 -> i at index i-1: the
+       arrays solve_specific_intensity (dIs) and solve_attenuated_emissivity
+       (transfer.py:89-144) take.  Rows after a ray stops are not written:
+       zero them first (the reference's frozen rows carry dt = 0). */
+    double *rows_em, *rows_ab, *rows_dt;
+    int64_t rows;
 } mk_request;
 
 /* ---------------------------------------------------------------- misc */

@@ -58,7 +58,7 @@ class Request(_c.Structure):
                 ("electron_gamma_m1", _D), ("ion_gamma_m1", _D), ("Ne_unit", _D), ("B_unit", _D),
                 ("L_unit", _D), ("cos_fallback_pitch", _D), ("sigma_cut", _D), ("nnu", _I32),
                 ("snapshot", _I32), ("nu", _D * MK_MAX_NU), ("image", _VP), ("nsteps", _VP), ("status", _VP),
-                ("ray_offset", _I64)]
+                ("ray_offset", _I64), ("rows_em", _VP), ("rows_ab", _VP), ("rows_dt", _VP), ("rows", _I64)]
 
 
 class Job(_c.Structure):

@@ -167,9 +167,12 @@ __device__ __forceinline__ void finish_ray(const mk_request &R, int64_t pix, con
 // folded into (I, P) for each frequency.  Returns without touching I, P
 // outside the snapshot, where the reference's zeroed primitives give
 // j = alpha = 0 exactly.
+// row >= 0: also store em and ab at that trajectory row of the request's
+// per-step diagnostic arrays (row < R.rows).
 __device__ __forceinline__ void sample_fp64(const mk_request &R, const mk_snapshot_view &sv, const double s[8],
                                             const KerrPoint<double> &m, double dt_used, double I[MK_MAX_NU],
-                                            double P[MK_MAX_NU], int &nsamples, double &max_tau) {
+                                            double P[MK_MAX_NU], int &nsamples, double &max_tau, int64_t pix,
+                                            int64_t row) {
     CellPos c;
     if (!locate(sv, s[1], s[2], s[3], c)) return;
     ++nsamples;
@@ -191,6 +194,11 @@ __device__ __forceinline__ void sample_fp64(const mk_request &R, const mk_snapsh
             double em, ab;
             synchro_eval(sp, -fs.kdotu * nu_obs, true, 1. / nu_obs, em, ab);
             if (cut) { em = 0.0; ab = 0.0; }
+            if (row >= 0) {
+                const int64_t at = (ch * R.rows + row) * request_pixels(R.camera) + pix;
+                R.rows_em[at] = em;
+                R.rows_ab[at] = ab;
+            }
             const double tau = w * ab;
             I[ch] += (w * em) * P[ch];
             P[ch] *= (1.0 - tau);
@@ -468,8 +476,15 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
                 dt = T(dtn);
                 ++steps;
                 ++fp64_steps;
-                if constexpr (SRC == SRC_CAMERA)
-                    sample_fp64(R, snaps[R.snapshot], s, m, dt_used, I, P, nsamples, max_tau);
+                if constexpr (SRC == SRC_CAMERA) {
+                    int64_t row = -1;
+                    if (R.rows_dt && steps < R.rows) {  // per-step diagnostics: row `steps` = this state
+                        row = steps;
+                        R.rows_dt[(int64_t)(steps - 1) * request_pixels(R.camera) + pix] = dt_used;
+                    }
+                    sample_fp64(R, snaps[R.snapshot], s, m, dt_used, I, P, nsamples, max_tau, pix,
+                                R.rows_em ? row : -1);
+                }
                 else {  // mixed form: FP64 (or pair) geodesic, FP32 emission, FP64 sums
                     const int ns0 = nsamples;
                     sample_f32_at(R, snaps[R.snapshot], sf, s, m, dt_used, I, P, sc, nsamples, max_tau);

@@ -19,7 +19,7 @@ from ._device import device, ptr, stream_ptr
 from .constants import JY, Msun
 from .geodesics import camera_pixels, make_camera, step_policy
 
-__all__ = ["make_image", "RenderRequest", "PreparedRender", "render_requests", "image_flux_jy"]
+__all__ = ["make_image", "RenderRequest", "PreparedRender", "render_requests", "image_flux_jy", "step_diagnostics"]
 
 PRECISIONS = {"fp64": _lib.MK_FP64, "mixed": _lib.MK_MIXED, "mixed_df": _lib.MK_MIXED_DF,
               "mixed_strict": _lib.MK_MIXED_STRICT}
@@ -42,6 +42,7 @@ class RenderRequest:
     bhspin: float = None               # default: the model's spin
     div: float = 40.
     tol: float = 1e-4
+    rows: int = 0                      # > 0: per-step diagnostic rows (FP64 form), see step_diagnostics
     out: dict = field(default_factory=dict)
 
     @property
@@ -53,7 +54,7 @@ class RenderRequest:
         return int(self.resolution) ** 2
 
 
-def _fill_request(req, rq, snap_index, image, nsteps, status, offset):
+def _fill_request(req, rq, snap_index, image, nsteps, status, offset, rows=None):
     model = req.model
     a = model.bhspin if req.bhspin is None else req.bhspin
     if model.fluid_gamma is None:
@@ -78,6 +79,9 @@ def _fill_request(req, rq, snap_index, image, nsteps, status, offset):
         rq.nu[i] = float(f)
     rq.image, rq.nsteps, rq.status = ptr(image), ptr(nsteps), ptr(status)
     rq.ray_offset = int(offset)
+    if rows is not None:
+        em, ab, dt = rows
+        rq.rows_em, rq.rows_ab, rq.rows_dt, rq.rows = ptr(em), ptr(ab), ptr(dt), int(dt.shape[0])
 
 
 class PreparedRender:
@@ -104,10 +108,21 @@ class PreparedRender:
         for i, r in enumerate(requests):
             img = torch.empty((len(r.freqs), r.resolution, r.resolution), dtype=torch.float64, device=dev)
             ns = st = None
-            if with_steps:
+            if with_steps or r.rows:
                 ns = torch.empty((r.resolution, r.resolution), dtype=torch.int32, device=dev)
                 st = torch.empty((r.resolution, r.resolution), dtype=torch.int32, device=dev)
-            _fill_request(r, table[i], snap_index[id(r.model.snapshot)], img, ns, st, offset)
+            rows = None
+            if r.rows:
+                if precision != "fp64":
+                    raise ValueError("per-step diagnostic rows come from the FP64 form only")
+                nr = min(int(r.rows), int(r.max_nsteps))
+                rows = (torch.zeros((len(r.freqs), nr, r.npx), dtype=torch.float64, device=dev),
+                        torch.zeros((len(r.freqs), nr, r.npx), dtype=torch.float64, device=dev),
+                        torch.zeros((nr, r.npx), dtype=torch.float64, device=dev))
+                r.out["rows_em"], r.out["rows_ab"], r.out["rows_dt"] = rows
+            _fill_request(r, table[i], snap_index[id(r.model.snapshot)], img, ns, st, offset, rows)
+            if r.rows and not with_steps:
+                r.out["nsteps"], r.out["status"] = ns, st
             r.out["image"] = img
             if with_steps:
                 r.out["nsteps"], r.out["status"] = ns, st
@@ -185,6 +200,36 @@ def make_image(fluid_model, camera_inclination=60, camera_distance=1000, mass_sc
     if np.ndim(observing_frequency) == 0:
         out = out[0]
     return out
+
+
+def step_diagnostics(fluid_model, camera_inclination=60, camera_distance=1000, mass_scale=1.e26,
+                     M_bh=6.2e9 * Msun, r_high=40, observing_frequency=230.e9, fov=20, resolution=160,
+                     max_nsteps=10000, r_low=1):
+    """make_image's per-step quantities from one fused FP64 launch.
+
+    Returns a dict of CUDA tensors: ``em`` and ``ab`` (nnu, N_t, npx), the
+    invariant emissivity and absorptivity at each trajectory row, ``dt``
+    (N_t, npx), trimmed to the N_t rows geodesic_integrator keeps
+    (geodesics.py:275-281); ``dIs`` (nnu, N_t - 1, npx), the per-step
+    intensity changes solve_specific_intensity(dIs=True) returns
+    (transfer.py:111-117, backward order), ``attenuated`` (nnu, N_t - 1,
+    npx), solve_attenuated_emissivity (transfer.py:122-144); ``image``
+    (nnu, res, res) and ``nsteps`` (res, res).  Rows after a ray stops hold
+    zeros where the reference repeats the frozen state's sample; both carry
+    dt = 0, so dIs and the attenuated emissivity agree there."""
+    from .geodesics import trimmed_rows
+    from .transfer import solve_attenuated_emissivity, solve_specific_intensity
+    req = RenderRequest(fluid_model, camera_inclination, camera_distance, mass_scale, M_bh, r_high,
+                        observing_frequency, fov, resolution, max_nsteps, r_low, rows=max_nsteps)
+    PreparedRender([req], precision="fp64").launch()
+    K = req.out["nsteps"].reshape(-1)
+    nt = trimmed_rows(K, max_nsteps)
+    em, ab, dt = req.out["rows_em"][:, :nt], req.out["rows_ab"][:, :nt], req.out["rows_dt"][:nt]
+    L_unit = fluid_model.get_units(M_bh, mass_scale)["L_unit"]
+    nnu = em.shape[0]
+    dIs = torch.stack([solve_specific_intensity(em[c], ab[c], dt, L_unit, dIs=True)[1] for c in range(nnu)])
+    att = torch.stack([solve_attenuated_emissivity(em[c], ab[c], dt, L_unit) for c in range(nnu)])
+    return dict(image=req.out["image"], nsteps=req.out["nsteps"], em=em, ab=ab, dt=dt, dIs=dIs, attenuated=att)
 
 
 def image_flux_jy(image, fov, distance_cm, L_unit):

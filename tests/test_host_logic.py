@@ -35,9 +35,10 @@ def test_trim_rule_on_reference_fixture():
 
 def test_request_struct_layout():
     from mahakala_gb300 import _lib
-    assert ctypes.sizeof(_lib.Request) == 272
+    assert ctypes.sizeof(_lib.Request) == 304
     assert ctypes.sizeof(_lib.SnapshotView) == 112
     assert _lib.Request.ray_offset.offset == 264
+    assert _lib.Request.rows.offset == 296
 
 
 def test_mass_scale_interpolation():
