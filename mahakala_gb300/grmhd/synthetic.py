@@ -140,3 +140,71 @@ def make_synthetic_snapshot(nblocks=16, cells_per_block=16, extent=50.0,
         params=dict(nblocks=nb, cells_per_block=n, extent=float(extent),
                     seed=int(seed), plasma_beta=float(plasma_beta),
                     noise_sigma=float(noise_sigma)))
+
+
+def _torus_fields(x, y, z, a, rng, fluid_gamma, plasma_beta, noise_sigma):
+    """The field model of the module docstring at cell centres (x, y, z)
+    (broadcast arrays); returns 8 float32 arrays dens, velx..velz, eint,
+    bcc1..3."""
+    r_h = 1.0 + np.sqrt(1.0 - a * a)
+    r = _ks_radius(x, y, z, a)
+    R = np.maximum(np.sqrt(x * x + y * y), 1e-12)
+    H = 0.4 * R
+    noise = rng.standard_normal(np.shape(r))
+    rho = (r / 6.0) ** -1.5 * np.exp(-z * z / (2.0 * H * H)) * np.exp(noise_sigma * noise)
+    u = 0.1 * rho / r
+    vk = 1.0 / np.sqrt(r)
+    phx, phy = -y / R, x / R
+    vr = -0.05 * vk
+    bmag = np.sqrt(2.0 * (fluid_gamma - 1.0) * u / plasma_beta)
+    out = (rho, vk * phx + vr * x / r, vk * phy + vr * y / r, vr * z / r, u,
+           0.8 * bmag * phx, 0.8 * bmag * phy, 0.6 * bmag)
+    inside = r < r_h
+    return [np.where(inside, 0.0, np.broadcast_to(v, np.shape(r))).astype(np.float32) for v in out]
+
+
+def make_multilevel_snapshot(nblocks=2, cells_per_block=8, extent=8.0, refine=((0, 0, 0, 0),),
+                             bhspin=0.94, seed=0, fluid_gamma=13.0 / 9.0, plasma_beta=10.0,
+                             noise_sigma=0.3):
+    """A mesh refined like AthenaK's static/adaptive refinement: nblocks^3
+    root blocks (level 0) of cells_per_block^3 cells over [-extent, extent]^3;
+    each entry (level, i, j, k) of ``refine``, applied in order, replaces that
+    block by its 8 children at level + 1 (logical locations 2i + {0,1}, ...).
+    Blocks are listed by level, then k, j, i.  Same field model as
+    make_synthetic_snapshot, evaluated at each block's own cell centres."""
+    nb, n = int(nblocks), int(cells_per_block)
+    blocks = {(0, i, j, k) for i in range(nb) for j in range(nb) for k in range(nb)}
+    for key in refine:
+        key = tuple(int(v) for v in key)
+        if key not in blocks:
+            raise ValueError(f"no block {key} to refine")
+        blocks.remove(key)
+        lv, i, j, k = key
+        for c in range(8):
+            blocks.add((lv + 1, 2 * i + (c & 1), 2 * j + ((c >> 1) & 1), 2 * k + (c >> 2)))
+    order = sorted(blocks, key=lambda b: (b[0], b[3], b[2], b[1]))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = float(bhspin)
+    nmb = len(order)
+    data = np.zeros((8, nmb, n, n, n), np.float32)
+    coords = {c: (np.zeros((nmb, n)), np.zeros((nmb, n + 1))) for c in range(3)}
+    for m, (lv, i, j, k) in enumerate(order):
+        w = 2.0 * extent / (nb * 2 ** lv)  # block width at this level
+        dx = w / n
+        cen, fac = [], []
+        for c, loc in enumerate((i, j, k)):
+            left = -extent + loc * w
+            v = left + (np.arange(n) + 0.5) * dx
+            f = left + np.arange(n + 1) * dx
+            coords[c][0][m], coords[c][1][m] = v, f
+            cen.append(v)
+        zz, yy, xx = np.meshgrid(cen[2], cen[1], cen[0], indexing="ij")
+        for p, arr in enumerate(_torus_fields(xx, yy, zz, a, rng, fluid_gamma, plasma_beta, noise_sigma)):
+            data[p, m] = arr
+    locs = np.array([[i, j, k] for _, i, j, k in order], np.int32)
+    levels = np.array([lv for lv, _, _, _ in order], np.int32)
+    return SnapshotArrays(uov=data[:5], B=data[5:], x1v=coords[0][0], x2v=coords[1][0], x3v=coords[2][0],
+                          x1f=coords[0][1], x2f=coords[1][1], x3f=coords[2][1], LogicalLocations=locs,
+                          Levels=levels, bhspin=a, fluid_gamma=float(fluid_gamma),
+                          params=dict(nblocks=nb, cells_per_block=n, extent=float(extent),
+                                      refine=[tuple(r) for r in refine], seed=int(seed)))

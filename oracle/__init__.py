@@ -331,41 +331,46 @@ def get_units(M_BH, mass_scale):
 class OracleSnapshot:
     """Ghost-filled meshblocks + geometry, as AthenakFluidModel holds them.
 
-    ``all_meshblocks`` is ``(nmb, 8, n+2, n+2, n+2)`` indexed
-    ``[mb, prim, k, j, i]`` (athenak.py:124-127) in float32 (the data are
-    float32 in origin, so the float64 promotion the reference performs is
-    exact).  Only single-level meshes are restated: the same-level ghost copy
-    of athenak.py:217-233, zero ghosts at the domain edge."""
+    ``all_meshblocks`` is ``(nmb, 8, n+2, n+2, n+2)`` float64 indexed
+    ``[mb, prim, k, j, i]`` (athenak.py:124-127, 145).  Single-level meshes
+    take the same-level ghost copy of athenak.py:217-233 (zero ghosts at the
+    domain edge); multi-level meshes the full fill of athenak.py:160-525
+    (``oracle.amr``), with the literal O(nmb) lookup."""
 
     def __init__(self, arrs, bhspin=None, fluid_gamma=None, fast_lookup=True):
         uov, B = arrs.uov, arrs.B
         nprim, nmb, nk, nj, ni = uov.shape
         if not (nk == nj == ni):
             raise NotImplementedError("cubic meshblocks only")
-        if np.any(np.asarray(arrs.Levels) != np.asarray(arrs.Levels)[0]):
-            raise NotImplementedError("single-level meshes only")
+        levels = np.asarray(arrs.Levels)
+        multilevel = bool(np.any(levels != levels[0]))
         n = ni
         self.n, self.nmb = n, nmb
         self.bhspin = float(arrs.bhspin if bhspin is None else bhspin)
         self.fluid_gamma = float(arrs.fluid_gamma if fluid_gamma is None else fluid_gamma)
         locs = np.asarray(arrs.LogicalLocations)
-        index = {tuple(int(v) for v in locs[m]): m for m in range(nmb)}
-        mbs = np.zeros((nmb, 8, n + 2, n + 2, n + 2), dtype=np.float32)
         data = np.concatenate([uov, B], axis=0)  # (8, nmb, k, j, i)
-        mbs[:, :, 1:-1, 1:-1, 1:-1] = data.transpose(1, 0, 2, 3, 4)
-        for m in range(nmb):
-            ti, tj, tk = (int(v) for v in locs[m])
-            for di in (-1, 0, 1):
-                for dj in (-1, 0, 1):
-                    for dk in (-1, 0, 1):
-                        if di == dj == dk == 0:
-                            continue
-                        nb = index.get((ti + di, tj + dj, tk + dk))
-                        if nb is None:
-                            continue
-                        src = [0 if d == 1 else (-1 if d == -1 else slice(0, n)) for d in (di, dj, dk)]
-                        tgt = [-1 if d == 1 else (0 if d == -1 else slice(1, n + 1)) for d in (di, dj, dk)]
-                        mbs[m, :, tgt[2], tgt[1], tgt[0]] = data[:, nb, src[2], src[1], src[0]]
+        if multilevel:
+            from .amr import multilevel_meshblocks
+            mbs = multilevel_meshblocks(data, locs, levels)
+            fast_lookup = False
+        else:
+            index = {tuple(int(v) for v in locs[m]): m for m in range(nmb)}
+            mbs = np.zeros((nmb, 8, n + 2, n + 2, n + 2), dtype=np.float64)
+            mbs[:, :, 1:-1, 1:-1, 1:-1] = data.transpose(1, 0, 2, 3, 4)
+            for m in range(nmb):
+                ti, tj, tk = (int(v) for v in locs[m])
+                for di in (-1, 0, 1):
+                    for dj in (-1, 0, 1):
+                        for dk in (-1, 0, 1):
+                            if di == dj == dk == 0:
+                                continue
+                            nb = index.get((ti + di, tj + dj, tk + dk))
+                            if nb is None:
+                                continue
+                            src = [0 if d == 1 else (-1 if d == -1 else slice(0, n)) for d in (di, dj, dk)]
+                            tgt = [-1 if d == 1 else (0 if d == -1 else slice(1, n + 1)) for d in (di, dj, dk)]
+                            mbs[m, :, tgt[2], tgt[1], tgt[0]] = data[:, nb, src[2], src[1], src[0]]
         self.all_meshblocks = mbs
         self.ext = _c(np.stack([arrs.x1f[:, 0], arrs.x1f[:, -1], arrs.x2f[:, 0], arrs.x2f[:, -1],
                                 arrs.x3f[:, 0], arrs.x3f[:, -1]], axis=1))
@@ -392,7 +397,7 @@ class OracleSnapshot:
 
     def _args(self):
         f = self.faces
-        return (_p(self.all_meshblocks, _F), ctypes.c_int(self.nmb), ctypes.c_int(self.n),
+        return (_p(self.all_meshblocks), ctypes.c_int(self.nmb), ctypes.c_int(self.n),
                 _p(self.ext), _p(self.left), _p(self.dx),
                 _p(f[0]) if f else None, _p(f[1]) if f else None, _p(f[2]) if f else None,
                 _p(self.nb, _I) if f else None, _p(self.table, _I) if f else None,

@@ -424,7 +424,7 @@ void orc_trace_fixed(const double *s0, int npx, int N, double a, double hfrac, d
 /* fluid sampling (grmhd/athenak.py:639-812)                            */
 /* ------------------------------------------------------------------ */
 typedef struct {
-    const float *mb;        /* (nmb, 8, n+2, n+2, n+2): [mb][prim][k][j][i] */
+    const double *mb;       /* (nmb, 8, n+2, n+2, n+2): [mb][prim][k][j][i], as the reference holds it */
     int nmb, n;
     const double *ext;      /* (nmb, 6): x1f[0], x1f[-1], x2f[0], x2f[-1], x3f[0], x3f[-1] */
     const double *left;     /* (nmb, 3): x1v[0], x2v[0], x3v[0] */
@@ -502,10 +502,10 @@ static int sample_prims(const orc_snapshot *m, const double *x, double *prims) {
         idx[c] = (int)py_floordiv(t, d);
     }
     int n2 = m->n + 2;
-    const float *base = m->mb + (int64_t)b * 8 * n2 * n2 * n2;
+    const double *base = m->mb + (int64_t)b * 8 * n2 * n2 * n2;
     for (int p = 0; p < 8; p++) {
-        const float *q = base + (int64_t)p * n2 * n2 * n2;
-#define AT(kk, jj, ii) ((double)q[((int64_t)(idx[2] + (kk)) * n2 + (idx[1] + (jj))) * n2 + (idx[0] + (ii))])
+        const double *q = base + (int64_t)p * n2 * n2 * n2;
+#define AT(kk, jj, ii) (q[((int64_t)(idx[2] + (kk)) * n2 + (idx[1] + (jj))) * n2 + (idx[0] + (ii))])
         double aaa = AT(0, 0, 0), aab = AT(0, 0, 1), aba = AT(0, 1, 0), abb = AT(0, 1, 1);
         double baa = AT(1, 0, 0), bab = AT(1, 0, 1), bba = AT(1, 1, 0), bbb = AT(1, 1, 1);
 #undef AT
@@ -555,7 +555,7 @@ static void fluid_scalars_point(const orc_snapshot *m, const double *S0, double 
     out[4] = sqrt(bdotb);
 }
 
-static void build_snapshot(orc_snapshot *m, const float *mb, int nmb, int n, const double *ext,
+static void build_snapshot(orc_snapshot *m, const double *mb, int nmb, int n, const double *ext,
                            const double *left, const double *dx, const double *f1, const double *f2,
                            const double *f3, const int32_t *nb, const int32_t *table, double a) {
     m->mb = mb; m->nmb = nmb; m->n = n; m->ext = ext; m->left = left; m->dx = dx;
@@ -565,7 +565,7 @@ static void build_snapshot(orc_snapshot *m, const float *mb, int nmb, int n, con
 }
 
 /* get_fluid_scalars_from_geodesics over npts points of S (npts x 8) */
-void orc_fluid_scalars(const float *mb, int nmb, int n, const double *ext, const double *left,
+void orc_fluid_scalars(const double *mb, int nmb, int n, const double *ext, const double *left,
                        const double *dx, const double *f1, const double *f2, const double *f3,
                        const int32_t *nb, const int32_t *table, double a,
                        const double *S, int64_t npts, double cos_fallback, double *out) {
@@ -576,7 +576,7 @@ void orc_fluid_scalars(const float *mb, int nmb, int n, const double *ext, const
 }
 
 /* get_prims_from_geodesics over npts points (out: npts x 8) and the block id */
-void orc_fluid_prims(const float *mb, int nmb, int n, const double *ext, const double *left,
+void orc_fluid_prims(const double *mb, int nmb, int n, const double *ext, const double *left,
                      const double *dx, const double *f1, const double *f2, const double *f3,
                      const int32_t *nb, const int32_t *table, double a,
                      const double *S, int64_t npts, double *out, int32_t *block) {
@@ -688,7 +688,7 @@ typedef struct {
 
 /* Renders npx rays from s0 (npx x 8).  image (nnu x npx).  nsteps[p] = the
    ray's accepted steps used by the transfer solve. */
-void orc_render(const orc_render_params *P, const float *mb, int nmb, int n, const double *ext,
+void orc_render(const orc_render_params *P, const double *mb, int nmb, int n, const double *ext,
                 const double *left, const double *dx, const double *f1, const double *f2,
                 const double *f3, const int32_t *nb, const int32_t *table,
                 const double *s0, int npx, double *image, int *nsteps) {

@@ -42,6 +42,17 @@ def tiny_arrays():
                           Levels=d["Levels"], bhspin=0.9, fluid_gamma=13. / 9)
 
 
+def amr_arrays(case):
+    """Multi-level synthetic mesh `case` (0 or 1) stored in tests/golden/amr.npz."""
+    from mahakala_gb300.grmhd.synthetic import SnapshotArrays
+    d = golden("amr")
+    p = f"case{case}_"
+    return SnapshotArrays(uov=d[p + "uov"], B=d[p + "B"], x1v=d[p + "x1v"], x2v=d[p + "x2v"], x3v=d[p + "x3v"],
+                          x1f=d[p + "x1f"], x2f=d[p + "x2f"], x3f=d[p + "x3f"],
+                          LogicalLocations=d[p + "LogicalLocations"], Levels=d[p + "Levels"], bhspin=0.94,
+                          fluid_gamma=13. / 9)
+
+
 @pytest.fixture(scope="session")
 def cuda():
     """Skip without a GPU; with one, build (if needed) and load the library."""

@@ -23,6 +23,8 @@ Fixtures:
                 tiny synthetic snapshot (grmhd/athenak.py:67-158)
   scalars       get_fluid_scalars_from_geodesics (grmhd/athenak.py:639-812)
   image         make_image (images.py:30-144) on the tiny snapshot
+  amr           two multi-level meshes: ghost fill (grmhd/athenak.py:67-525),
+                sampled primitives and scalars (:527-812), one image
 """
 
 import os
@@ -315,10 +317,68 @@ def gen_image():
     _save("image", **out)
 
 
+AMR_CASES = [
+    # three levels: a root block refined, one of its children refined again
+    dict(nblocks=2, cells_per_block=4, extent=8.0, refine=((0, 0, 0, 0), (1, 0, 0, 0)), seed=5),
+    # two refined root blocks meeting at an edge
+    dict(nblocks=2, cells_per_block=4, extent=8.0, refine=((0, 0, 0, 0), (0, 1, 1, 1)), seed=6),
+]
+AMR_IMAGE = dict(camera_inclination=50, camera_distance=1000, mass_scale=1e27, M_bh=6.2e9 * Msun, r_high=10,
+                 observing_frequency=230e9, fov=14, resolution=5, max_nsteps=1500)
+
+
+def _amr_model(case, fluid_gamma=13. / 9):
+    from mahakala_gb300.grmhd.synthetic import make_multilevel_snapshot
+    snap = make_multilevel_snapshot(**case)
+    name = "amr_synthetic_%d.athdf" % case["seed"]
+    datasets = dict(uov=snap.uov, B=snap.B, x1v=snap.x1v, x2v=snap.x2v, x3v=snap.x3v,
+                    x1f=snap.x1f, x2f=snap.x2f, x3f=snap.x3f,
+                    LogicalLocations=snap.LogicalLocations, Levels=snap.Levels)
+    attrs = {"VariableNames": np.array([v.encode() for v in snap.VariableNames])}
+    jaxshim.register_h5(name, datasets, attrs)
+    return snap, AthenakFluidModel(name, snap.bhspin, fluid_gamma=fluid_gamma)
+
+
+def gen_amr():
+    """Multi-level meshes: the reference's ghost fill (athenak.py:67-525),
+    its lookup + interpolation on sample points (:527-812) and one image."""
+    out = {}
+    rng = np.random.Generator(np.random.PCG64(77))
+    for c, case in enumerate(AMR_CASES):
+        snap, model = _amr_model(case)
+        ext = case["extent"]
+        S = _scalar_points(rng, 40, 10, ext, snap.bhspin)
+        faces = np.array([-ext, -ext / 2, -ext / 4, 0.0, ext / 4, ext / 2, ext])  # faces of every level
+        S[25:35, :, 0] = rng.choice(faces, (10, 10))
+        S[25:35, :, 1] = rng.choice(faces, (10, 10))
+        with np.errstate(all="ignore"):
+            sc = model.get_fluid_scalars_from_geodesics(S.view(J))
+            pr = model.get_prims_from_geodesics(S.view(J))
+        p = f"case{c}_"
+        for k in ("uov", "B", "x1v", "x2v", "x3v", "x1f", "x2f", "x3f", "LogicalLocations", "Levels"):
+            out[p + k] = getattr(snap, k)
+        out[p + "all_meshblocks"] = np.asarray(model.all_meshblocks)
+        out[p + "S"] = S
+        for k in ("dens", "u", "pitch_angle", "kdotu", "b"):
+            out[p + "sc_" + k] = np.asarray(sc[k])
+        for k in ("dens", "u", "U1", "U2", "U3", "B1", "B2", "B3"):
+            out[p + "pr_" + k] = np.asarray(pr[k])
+        if c == 0:
+            with np.errstate(all="ignore"):
+                out[p + "image"] = np.asarray(make_image(model, **AMR_IMAGE))
+            out[p + "image_kw"] = np.array([AMR_IMAGE[k] for k in ("camera_inclination", "camera_distance",
+                                                                   "mass_scale", "M_bh", "r_high",
+                                                                   "observing_frequency", "fov", "resolution",
+                                                                   "max_nsteps")])
+    out["params"] = np.array([[case["nblocks"], case["cells_per_block"], case["extent"], case["seed"]]
+                              for case in AMR_CASES])
+    _save("amr", **out)
+
+
 GENERATORS = dict(camera=gen_camera, integrator=gen_integrator, shadow=gen_shadow,
                   synchrotron=gen_synchrotron, electrons=gen_electrons,
                   transfer=gen_transfer, units=gen_units, snapshot=gen_snapshot,
-                  scalars=gen_scalars, image=gen_image)
+                  scalars=gen_scalars, image=gen_image, amr=gen_amr)
 
 
 if __name__ == "__main__":
