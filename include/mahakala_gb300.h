@@ -86,17 +86,47 @@ typedef struct {
 
 /* Device view of one resident snapshot (meshblocks with one ghost layer,
    AoS float32 [mb][k][j][i][prim], prim order dens, velx, vely, velz, eint,
-   bcc1, bcc2, bcc3).  Filled by mk_snapshot_build; plain data, copyable. */
+   bcc1, bcc2, bcc3), single- or multi-level.  Filled by mk_snapshot_build;
+   plain data, copyable. */
 typedef struct {
     const float *blocks;     /* (nmb, n+2, n+2, n+2, 8) */
     const double *geom;      /* (nmb, 6): x1v[0], x2v[0], x3v[0], dx1, dx2, dx3 per block */
     const float *geom_f32;   /* (nmb, 8): x1v[0], x2v[0], x3v[0], 1/dx1, 1/dx2, 1/dx3, 0, 0 (mixed form) */
-    const double *faces;     /* block faces: nb[0]+1, then nb[1]+1, then nb[2]+1 values */
-    const int32_t *table;    /* (nb[2], nb[1], nb[0]) block id at each logical location */
+    const double *faces;     /* (nmb, 6): x1f[0], x1f[n], x2f[0], x2f[n], x3f[0], x3f[n] per block */
+    const int32_t *table;    /* (nb[2], nb[1], nb[0]) block covering each cell of the finest-level
+                                block grid, -1 where no block is */
+    const double *blocks64;  /* (n64, n+2, n+2, n+2, 8) binary64 copies of the blocks whose ghost
+                                cells average finer cells (their means are not float32 values), or
+                                NULL when no block has such ghosts */
+    const int32_t *block64;  /* (nmb) row of blocks64 for each block or -1; NULL with blocks64 */
     int32_t nmb, n;
     int32_t nb[3], pad0;
-    double lo[3], width[3];  /* first face and mean block width per axis (lookup guess) */
+    double lo[3], width[3];  /* first face and finest block width per axis */
 } mk_snapshot_view;
+
+/* Key of a block in a mesh's sorted key list: level and logical location
+   (i, j, k), each location < 2^18, level < 2^9. */
+#define MK_MESH_KEY(level, i, j, k)                                                                   \
+    (((int64_t)(level) << 54) | ((int64_t)(i) << 36) | ((int64_t)(j) << 18) | (int64_t)(k))
+
+/* A mesh for mk_snapshot_build (device pointers, kept by reference except
+   uov/B/locs/levels/keys, which are read only during the build). */
+typedef struct {
+    const float *uov;        /* (5, nmb, n, n, n) float32: dens, velx, vely, velz, eint */
+    const float *B;          /* (3, nmb, n, n, n) float32: bcc1..3 */
+    const int32_t *locs;     /* (nmb, 3) logical locations (i, j, k) at each block's level */
+    const int32_t *levels;   /* (nmb) refinement levels */
+    const int64_t *keys;     /* (nmb) MK_MESH_KEY of every block, ascending */
+    const int32_t *key_block;/* (nmb) block of each sorted key */
+    const double *geom;      /* as mk_snapshot_view.geom */
+    const double *faces;     /* as mk_snapshot_view.faces */
+    const int32_t *table;    /* as mk_snapshot_view.table */
+    double *blocks64;        /* storage for n64 binary64 blocks, or NULL (n64 = 0) */
+    const int32_t *block64;  /* (nmb) row of blocks64 or -1, or NULL */
+    int32_t nmb, n, n64, pad0;
+    int32_t nb[3], pad1;
+    double lo[3], width[3];
+} mk_mesh_desc;
 
 /* One render request: the arguments of make_image (images.py:30-35) after
    the host-side scalar prologue (units, grmhd/grmhd.py:40-55). */
@@ -184,15 +214,15 @@ int mk_shadow_pass(const double *cos_dev, const double *sin_dev, const double *m
 size_t mk_snapshot_bytes(int32_t nmb, int32_t n);
 
 /* Builds the ghost-filled AoS meshblocks on the device from AthenaK arrays
-   (load_athenak_meshblocks, grmhd/athenak.py:67-158; same-level ghost copy
-   :217-233, zero ghosts at the domain edge).  uov_dev (5, nmb, n, n, n) and
-   B_dev (3, nmb, n, n, n) float32; geom_dev (nmb, 6), faces_dev and
-   table_dev as in mk_snapshot_view (kept by reference, not copied);
-   locs_dev (nmb, 3) logical locations.  Single-level meshes only. */
-int mk_snapshot_build(const float *uov_dev, const float *B_dev, const int32_t *locs_dev,
-                      const double *geom_dev, const double *faces_dev, const int32_t *table_dev,
-                      int32_t nmb, int32_t n, const int32_t nb[3], const double lo[3],
-                      const double width[3], void *storage_dev, size_t storage_bytes,
+   (load_athenak_meshblocks, grmhd/athenak.py:67-158 with the multi-level
+   ghost fill of :160-525): a ghost region takes the same-level neighbour's
+   cells, else the coarser neighbour's (each coarse cell copied to the fine
+   ghosts it covers), else the mean of the finer neighbours' 2x2x2 cells
+   summed in binary64 in the reference's term order (including its first
+   edge term, which reads one cell), else zero.  Means are stored rounded to
+   float32 in `blocks` and exactly in `blocks64` for the FP64 path.  storage
+   >= mk_snapshot_bytes(nmb, n), 16-byte aligned. */
+int mk_snapshot_build(const mk_mesh_desc *mesh, void *storage_dev, size_t storage_bytes,
                       mk_snapshot_view *view_out, void *stream);
 
 /* ------------------------------------------------------ stage kernels */

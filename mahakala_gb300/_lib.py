@@ -7,6 +7,8 @@ no CPU fallback; a missing library or a missing GPU raises immediately.
 import ctypes
 import os
 
+import numpy as np
+
 from . import build as _build
 
 _c = ctypes
@@ -48,9 +50,21 @@ class Camera(_c.Structure):
 
 
 class SnapshotView(_c.Structure):
-    _fields_ = [("blocks", _VP), ("geom", _VP), ("geom_f32", _VP), ("faces", _VP), ("table", _VP), ("nmb", _I32),
-                ("n", _I32),
+    _fields_ = [("blocks", _VP), ("geom", _VP), ("geom_f32", _VP), ("faces", _VP), ("table", _VP),
+                ("blocks64", _VP), ("block64", _VP), ("nmb", _I32), ("n", _I32),
                 ("nb", _I32 * 3), ("pad0", _I32), ("lo", _D * 3), ("width", _D * 3)]
+
+
+class MeshDesc(_c.Structure):
+    _fields_ = [("uov", _VP), ("B", _VP), ("locs", _VP), ("levels", _VP), ("keys", _VP), ("key_block", _VP),
+                ("geom", _VP), ("faces", _VP), ("table", _VP), ("blocks64", _VP), ("block64", _VP),
+                ("nmb", _I32), ("n", _I32), ("n64", _I32), ("pad0", _I32), ("nb", _I32 * 3), ("pad1", _I32),
+                ("lo", _D * 3), ("width", _D * 3)]
+
+
+def mesh_key(level, i, j, k):
+    """MK_MESH_KEY of include/mahakala_gb300.h (NumPy arrays or ints)."""
+    return (np.int64(level) << 54) | (np.int64(i) << 36) | (np.int64(j) << 18) | np.int64(k)
 
 
 class Request(_c.Structure):
@@ -78,8 +92,7 @@ SIGNATURES = {
     "mk_shadow_pass": (_c.c_int, [_VP, _VP, _VP, _I64, _D, _D, _D, _D, _I32, _VP, _VP, _VP, _VP, _VP, _VP,
                                   _VP]),
     "mk_snapshot_bytes": (_SZ, [_I32, _I32]),
-    "mk_snapshot_build": (_c.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _I32 * 3, _D * 3, _D * 3, _VP,
-                                     _SZ, _c.POINTER(SnapshotView), _VP]),
+    "mk_snapshot_build": (_c.c_int, [_c.POINTER(MeshDesc), _VP, _SZ, _c.POINTER(SnapshotView), _VP]),
     "mk_fluid_scalars": (_c.c_int, [_c.POINTER(SnapshotView), _D, _VP, _I64, _D, _VP, _VP]),
     "mk_fluid_prims": (_c.c_int, [_c.POINTER(SnapshotView), _VP, _I64, _VP, _VP, _VP]),
     "mk_rlow_rhigh": (_c.c_int, [_VP, _VP, _VP, _I64, _D, _D, _D, _D, _VP, _VP]),
@@ -119,7 +132,7 @@ def load():
         fn.restype = res
         fn.argtypes = args
     for name, cls in (("mk_step_policy", StepPolicy), ("mk_camera", Camera),
-                      ("mk_snapshot_view", SnapshotView), ("mk_request", Request)):
+                      ("mk_snapshot_view", SnapshotView), ("mk_mesh_desc", MeshDesc), ("mk_request", Request)):
         n = lib.mk_sizeof(name.encode())
         if n != _c.sizeof(cls):
             raise RuntimeError(f"ABI mismatch: sizeof({name}) C={n} ctypes={_c.sizeof(cls)}")

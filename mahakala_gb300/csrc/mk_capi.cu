@@ -38,6 +38,7 @@ extern "C" size_t mk_sizeof(const char *name) {
     if (!strcmp(name, "mk_step_policy")) return sizeof(mk_step_policy);
     if (!strcmp(name, "mk_camera")) return sizeof(mk_camera);
     if (!strcmp(name, "mk_snapshot_view")) return sizeof(mk_snapshot_view);
+    if (!strcmp(name, "mk_mesh_desc")) return sizeof(mk_mesh_desc);
     if (!strcmp(name, "mk_request")) return sizeof(mk_request);
     return 0;
 }

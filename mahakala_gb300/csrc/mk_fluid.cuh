@@ -12,26 +12,67 @@
 namespace mk {
 
 // ------------------------------------------------------------- lookup
-// block index b along one axis with faces[b] < x <= faces[b+1], -1 outside
-// (the per-axis form of athenak.py:663-670 on a single-level mesh)
-__device__ __forceinline__ int axis_block(const double *__restrict__ faces, int nb, double lo,
-                                          double width, double x) {
-    if (!(x > __ldg(faces) && x <= __ldg(faces + nb))) return -1;
-    int b = (int)floor((x - lo) / width);
-    b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
-    for (int it = 0; it < nb && x <= __ldg(faces + b); ++it) --b;
-    for (int it = 0; it < nb && x > __ldg(faces + b + 1); ++it) ++b;
-    return b;
+// The block with left < x <= right on all three axes, the last such block
+// when several are (athenak.py:657-670 scans them all), -1 for none.  The
+// finest-level table gives the candidate; the exact face test decides, and
+// a point within rounding of the candidate's faces is moved one table cell
+// across them until the test holds.  Blocks that tile the domain leave at
+// most one block passing; where two do (faces an ulp apart) the higher
+// index wins, as in the scan.
+__device__ __forceinline__ bool in_block(const double *__restrict__ f, double x, double y, double z) {
+    return x > __ldg(f) && x <= __ldg(f + 1) && y > __ldg(f + 2) && y <= __ldg(f + 3) && z > __ldg(f + 4) &&
+           z <= __ldg(f + 5);
+}
+
+__device__ __forceinline__ int table_at(const mk_snapshot_view &s, const int c[3]) {
+    if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= s.nb[0] || c[1] >= s.nb[1] || c[2] >= s.nb[2]) return -1;
+    return __ldg(s.table + ((int64_t)c[2] * s.nb[1] + c[1]) * s.nb[0] + c[0]);
 }
 
 __device__ __forceinline__ int find_block(const mk_snapshot_view &s, double x, double y, double z) {
-    const int bi = axis_block(s.faces, s.nb[0], s.lo[0], s.width[0], x);
-    if (bi < 0) return -1;
-    const int bj = axis_block(s.faces + s.nb[0] + 1, s.nb[1], s.lo[1], s.width[1], y);
-    if (bj < 0) return -1;
-    const int bk = axis_block(s.faces + s.nb[0] + s.nb[1] + 2, s.nb[2], s.lo[2], s.width[2], z);
-    if (bk < 0) return -1;
-    return __ldg(s.table + ((int64_t)bk * s.nb[1] + bj) * s.nb[0] + bi);
+    const double xs[3] = {x, y, z};
+    int c[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double u = floor((xs[a] - s.lo[a]) / s.width[a]);
+        if (!(u >= -1.0 && u <= (double)s.nb[a])) return -1;  // far outside (or NaN)
+        c[a] = (int)u < 0 ? 0 : ((int)u >= s.nb[a] ? s.nb[a] - 1 : (int)u);
+    }
+    int mb = -1;
+    for (int it = 0; it < 4; ++it) {
+        mb = table_at(s, c);
+        if (mb < 0) return -1;
+        const double *f = s.faces + 6 * (int64_t)mb;
+        bool moved = false;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (xs[a] <= __ldg(f + 2 * a)) { --c[a]; moved = true; }
+            else if (xs[a] > __ldg(f + 2 * a + 1)) { ++c[a]; moved = true; }
+        }
+        if (!moved) break;
+        if (it == 3) return -1;
+    }
+    if (mb < 0) return -1;
+    // neighbours across a face the point lies on (to rounding) that also
+    // pass the test: the scan keeps the last
+    const double *f = s.faces + 6 * (int64_t)mb;
+    int lo_[3], hi_[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double w = __ldg(f + 2 * a + 1) - __ldg(f + 2 * a);
+        lo_[a] = xs[a] - __ldg(f + 2 * a) <= 1e-12 * w ? -1 : 0;
+        hi_[a] = __ldg(f + 2 * a + 1) - xs[a] <= 1e-12 * w ? 1 : 0;
+    }
+    if (lo_[0] | hi_[0] | lo_[1] | hi_[1] | lo_[2] | hi_[2]) {
+        for (int dk = lo_[2]; dk <= hi_[2]; dk++)
+            for (int dj = lo_[1]; dj <= hi_[1]; dj++)
+                for (int di = lo_[0]; di <= hi_[0]; di++) {
+                    const int cc[3] = {c[0] + di, c[1] + dj, c[2] + dk};
+                    const int o = table_at(s, cc);
+                    if (o > mb && in_block(s.faces + 6 * (int64_t)o, x, y, z)) mb = o;
+                }
+    }
+    return mb;
 }
 
 // float floor_divide / remainder with NumPy (= jnp) semantics
@@ -79,23 +120,40 @@ __device__ __forceinline__ bool locate(const mk_snapshot_view &s, double x, doub
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
-// trilinear interpolation of the 8 primitives (athenak.py:737-752), FP64
+// trilinear interpolation of the 8 primitives (athenak.py:737-752), FP64.
+// Blocks whose ghosts average finer cells are read from their binary64 copy
+// (the means are not float32 values; the reference holds them in float64).
 __device__ __forceinline__ void trilinear8(const mk_snapshot_view &s, const CellPos &c, double prim[8]) {
     const int n2 = s.n + 2;
     const int64_t sj = (int64_t)n2 * 8, sk = (int64_t)n2 * n2 * 8;
-    const float *base = s.blocks + ((((int64_t)c.mb * n2 + c.idx[2]) * n2 + c.idx[1]) * n2 + c.idx[0]) * 8;
-    float v[2][2][2][8];
+    const int64_t at = ((((int64_t)c.mb * n2 + c.idx[2]) * n2 + c.idx[1]) * n2 + c.idx[0]) * 8;
+    const int row = s.blocks64 ? __ldg(s.block64 + c.mb) : -1;
+    double v[2][2][2][8];
+    if (row >= 0) {
+        const double *base = s.blocks64 + at + ((int64_t)row - c.mb) * n2 * n2 * n2 * 8;
 #pragma unroll
-    for (int dk = 0; dk < 2; dk++)
+        for (int dk = 0; dk < 2; dk++)
 #pragma unroll
-        for (int dj = 0; dj < 2; dj++)
+            for (int dj = 0; dj < 2; dj++)
 #pragma unroll
-            for (int di = 0; di < 2; di++) {
-                const float *p = base + dk * sk + dj * sj + di * 8;
-                const float4 lo = ldg4(p), hi = ldg4(p + 4);
-                v[dk][dj][di][0] = lo.x; v[dk][dj][di][1] = lo.y; v[dk][dj][di][2] = lo.z; v[dk][dj][di][3] = lo.w;
-                v[dk][dj][di][4] = hi.x; v[dk][dj][di][5] = hi.y; v[dk][dj][di][6] = hi.z; v[dk][dj][di][7] = hi.w;
-            }
+                for (int di = 0; di < 2; di++)
+#pragma unroll
+                    for (int p = 0; p < 8; p++) v[dk][dj][di][p] = __ldg(base + dk * sk + dj * sj + di * 8 + p);
+    } else {
+        const float *base = s.blocks + at;
+#pragma unroll
+        for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+            for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+                for (int di = 0; di < 2; di++) {
+                    const float *p = base + dk * sk + dj * sj + di * 8;
+                    const float4 lo = ldg4(p), hi = ldg4(p + 4);
+                    v[dk][dj][di][0] = lo.x; v[dk][dj][di][1] = lo.y; v[dk][dj][di][2] = lo.z;
+                    v[dk][dj][di][3] = lo.w; v[dk][dj][di][4] = hi.x; v[dk][dj][di][5] = hi.y;
+                    v[dk][dj][di][6] = hi.z; v[dk][dj][di][7] = hi.w;
+                }
+    }
     const double d1 = c.del[0], d2 = c.del[1], d3 = c.del[2];
     // a + (b - a) d rounded twice (no fused multiply-add), as the reference
     // evaluates it, so the interpolated primitives are bit-identical

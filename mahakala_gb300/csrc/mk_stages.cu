@@ -8,49 +8,125 @@
 
 namespace mk {
 
-// ghost-filled AoS meshblocks from AthenaK arrays: one thread per padded
-// cell (mb, k, j, i); same-level neighbour copy, zeros at the domain edge
-// (grmhd/athenak.py:108-127, 217-233)
-__global__ void snapshot_build_kernel(const float *__restrict__ uov, const float *__restrict__ B,
-                                      const int32_t *__restrict__ locs, const int32_t *__restrict__ table, int nmb,
-                                      int n, int nb0, int nb1, int nb2, float *__restrict__ out) {
-    const int n2 = n + 2;
-    const int64_t total = (int64_t)nmb * n2 * n2 * n2;
+// Block of a mesh at (level, i, j, k) by binary search of the sorted keys,
+// -1 if there is none (negative or out-of-range locations included).
+__device__ __forceinline__ int mesh_find(const int64_t *__restrict__ keys, const int32_t *__restrict__ key_block,
+                                         int nmb, int lv, int i, int j, int k) {
+    const int lim = 1 << 18;
+    if (lv < 0 || lv >= 512 || i < 0 || j < 0 || k < 0 || i >= lim || j >= lim || k >= lim) return -1;
+    const int64_t want = MK_MESH_KEY(lv, i, j, k);
+    int lo = 0, hi = nmb - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int64_t v = keys[mid];
+        if (v == want) return key_block[mid];
+        if (v < want) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ int py_floordiv2(int x) { return x >= 0 ? x / 2 : -((1 - x) / 2); }
+
+// One ghost-filled meshblock cell: one thread per padded cell (mb, k, j, i).
+// The ghost rules of load_athenak_meshblocks (grmhd/athenak.py:108-158,
+// 208-525), in order: same-level neighbour (copy of its adjacent cells);
+// coarser neighbour (each coarse cell copied to the 2 fine ghosts it covers
+// per transverse axis, the half chosen by the parity of t + d); finer
+// neighbours (mean of 2x2x2 fine cells: eight terms value/8 in float32,
+// summed in binary64, i over j over k, where an edge region's transverse
+// source is one cell for the first term and then the every-other-cell
+// offset of the previous term, as the reference's loop reads it); zero.
+__global__ void snapshot_build_kernel(mk_mesh_desc m, float *__restrict__ out) {
+    const int n = m.n, n2 = n + 2, h = n / 2;
+    const int64_t total = (int64_t)m.nmb * n2 * n2 * n2;
     const int64_t cell = (int64_t)n * n * n;
+    const int64_t pstride = (int64_t)m.nmb * cell;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t t = e;
-        const int i = (int)(t % n2); t /= n2;
-        const int j = (int)(t % n2); t /= n2;
-        const int k = (int)(t % n2); t /= n2;
-        const int mb = (int)t;
-        const int di = i == 0 ? -1 : (i == n + 1 ? 1 : 0);
-        const int dj = j == 0 ? -1 : (j == n + 1 ? 1 : 0);
-        const int dk = k == 0 ? -1 : (k == n + 1 ? 1 : 0);
-        int src = mb;
-        if (di || dj || dk) {
-            const int ti = locs[3 * mb] + di, tj = locs[3 * mb + 1] + dj, tk = locs[3 * mb + 2] + dk;
-            src = (ti < 0 || tj < 0 || tk < 0 || ti >= nb0 || tj >= nb1 || tk >= nb2)
-                      ? -1
-                      : table[((int64_t)tk * nb1 + tj) * nb0 + ti];
-        }
-        float v[8];
-        if (src < 0) {
+        int64_t q = e;
+        int c[3];
+        c[0] = (int)(q % n2); q /= n2;
+        c[1] = (int)(q % n2); q /= n2;
+        c[2] = (int)(q % n2); q /= n2;
+        const int mb = (int)q;
+        int d[3];
 #pragma unroll
-            for (int p = 0; p < 8; p++) v[p] = 0.0f;
+        for (int a = 0; a < 3; a++) d[a] = c[a] == 0 ? -1 : (c[a] == n + 1 ? 1 : 0);
+        double v[8];
+        auto load = [&](int blk, const int src[3], int p) -> float {
+            const int64_t off = (int64_t)blk * cell + ((int64_t)src[2] * n + src[1]) * n + src[0];
+            return p < 5 ? m.uov[(int64_t)p * pstride + off] : m.B[(int64_t)(p - 5) * pstride + off];
+        };
+        if (!(d[0] || d[1] || d[2])) {
+            const int src[3] = {c[0] - 1, c[1] - 1, c[2] - 1};
+#pragma unroll
+            for (int p = 0; p < 8; p++) v[p] = (double)load(mb, src, p);
         } else {
-            const int si = di == 1 ? 0 : (di == -1 ? n - 1 : i - 1);
-            const int sj = dj == 1 ? 0 : (dj == -1 ? n - 1 : j - 1);
-            const int sk = dk == 1 ? 0 : (dk == -1 ? n - 1 : k - 1);
-            const int64_t off = (int64_t)src * cell + ((int64_t)sk * n + sj) * n + si;
+            const int lv = m.levels[mb];
+            const int t[3] = {m.locs[3 * mb], m.locs[3 * mb + 1], m.locs[3 * mb + 2]};
+            int nb = mesh_find(m.keys, m.key_block, m.nmb, lv, t[0] + d[0], t[1] + d[1], t[2] + d[2]);
+            if (nb >= 0) {  // same level
+                int src[3];
 #pragma unroll
-            for (int p = 0; p < 5; p++) v[p] = uov[(int64_t)p * nmb * cell + off];
+                for (int a = 0; a < 3; a++) src[a] = d[a] == 1 ? 0 : (d[a] == -1 ? n - 1 : c[a] - 1);
 #pragma unroll
-            for (int p = 0; p < 3; p++) v[5 + p] = B[(int64_t)p * nmb * cell + off];
+                for (int p = 0; p < 8; p++) v[p] = (double)load(nb, src, p);
+            } else if ((nb = mesh_find(m.keys, m.key_block, m.nmb, lv - 1, py_floordiv2(t[0] + d[0]),
+                                       py_floordiv2(t[1] + d[1]), py_floordiv2(t[2] + d[2]))) >= 0) {
+                int src[3];  // coarser neighbour
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const int odd = (t[a] + d[a]) & 1;  // == Python's % 2 for either sign
+                    src[a] = d[a] == 1 ? (odd ? h : 0) : (d[a] == -1 ? (odd ? n - 1 : h - 1) : (odd ? h : 0) + (c[a] - 1) / 2);
+                }
+#pragma unroll
+                for (int p = 0; p < 8; p++) v[p] = (double)load(nb, src, p);
+            } else if (mesh_find(m.keys, m.key_block, m.nmb, lv + 1, 2 * (t[0] + d[0]), 2 * (t[1] + d[1]),
+                                 2 * (t[2] + d[2])) >= 0) {
+                // finer neighbours: the fine block holding this ghost cell's 2x2x2 cells
+                int blk[3], s0[3], mz[3], nz = 0;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    nz += d[a] != 0;
+                    const int ep = d[a] == 0 ? (c[a] - 1) / h : 0;
+                    blk[a] = 2 * (t[a] + d[a]) + (d[a] == -1 ? 1 : 0) + ep;
+                    s0[a] = d[a] == -1 ? n - 2 : 0;
+                    mz[a] = d[a] == 0 ? (c[a] - 1) - ep * h : 0;
+                }
+                nb = mesh_find(m.keys, m.key_block, m.nmb, lv + 1, blk[0], blk[1], blk[2]);
+#pragma unroll
+                for (int p = 0; p < 8; p++) v[p] = 0.0;
+                if (nb >= 0) {
+                    int prev[3] = {0, 0, 0};
+                    for (int step = 0; step < 8; step++) {
+                        const int w[3] = {(step >> 2) & 1, (step >> 1) & 1, step & 1};
+                        int src[3];
+#pragma unroll
+                        for (int a = 0; a < 3; a++) {
+                            if (d[a] != 0) src[a] = s0[a] + w[a];
+                            else if (nz == 2) src[a] = step == 0 ? 0 : prev[a] + 2 * mz[a];
+                            else src[a] = w[a] + 2 * mz[a];
+                        }
+#pragma unroll
+                        for (int p = 0; p < 8; p++) v[p] += (double)(load(nb, src, p) / 8.0f);
+#pragma unroll
+                        for (int a = 0; a < 3; a++) prev[a] = w[a];
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int p = 0; p < 8; p++) v[p] = 0.0;
+            }
         }
         float4 *o = reinterpret_cast<float4 *>(out + e * 8);
-        o[0] = make_float4(v[0], v[1], v[2], v[3]);
-        o[1] = make_float4(v[4], v[5], v[6], v[7]);
+        o[0] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+        o[1] = make_float4((float)v[4], (float)v[5], (float)v[6], (float)v[7]);
+        if (m.blocks64 && m.block64[mb] >= 0) {
+            double *o64 = m.blocks64 + ((int64_t)m.block64[mb] * n2 * n2 * n2 + (e - (int64_t)mb * n2 * n2 * n2)) * 8;
+#pragma unroll
+            for (int p = 0; p < 8; p++) o64[p] = v[p];
+        }
     }
 }
 
@@ -170,43 +246,45 @@ extern "C" size_t mk_snapshot_bytes(int32_t nmb, int32_t n) {
     return blocks_bytes(nmb, n) + (size_t)nmb * 8 * sizeof(float);
 }
 
-extern "C" int mk_snapshot_build(const float *uov_dev, const float *B_dev, const int32_t *locs_dev,
-                                 const double *geom_dev, const double *faces_dev, const int32_t *table_dev,
-                                 int32_t nmb, int32_t n, const int32_t nb[3], const double lo[3],
-                                 const double width[3], void *storage_dev, size_t storage_bytes,
+extern "C" int mk_snapshot_build(const mk_mesh_desc *mesh, void *storage_dev, size_t storage_bytes,
                                  mk_snapshot_view *view_out, void *stream) {
-    MK_REQUIRE(uov_dev && B_dev && locs_dev && geom_dev && faces_dev && table_dev && nb && lo && width &&
-                   storage_dev && view_out,
-               MK_ERR_ARG, "mk_snapshot_build: null pointer");
-    MK_REQUIRE(nmb > 0 && n >= 2, MK_ERR_ARG, "mk_snapshot_build: need nmb > 0 and n >= 2");
-    MK_REQUIRE(nb[0] > 0 && nb[1] > 0 && nb[2] > 0 && (int64_t)nb[0] * nb[1] * nb[2] >= nmb, MK_ERR_ARG,
-               "mk_snapshot_build: block grid too small");
-    MK_REQUIRE(storage_bytes >= mk_snapshot_bytes(nmb, n), MK_ERR_ARG,
-               "mk_snapshot_build: storage of %zu bytes, need %zu", storage_bytes, mk_snapshot_bytes(nmb, n));
+    MK_REQUIRE(mesh && storage_dev && view_out, MK_ERR_ARG, "mk_snapshot_build: null pointer");
+    const mk_mesh_desc &m = *mesh;
+    MK_REQUIRE(m.uov && m.B && m.locs && m.levels && m.keys && m.key_block && m.geom && m.faces && m.table,
+               MK_ERR_ARG, "mk_snapshot_build: null mesh array");
+    MK_REQUIRE(m.nmb > 0 && m.n >= 2 && m.n % 2 == 0, MK_ERR_ARG,
+               "mk_snapshot_build: need nmb > 0 and an even n >= 2 (n = %d)", (int)m.n);
+    MK_REQUIRE(m.nb[0] > 0 && m.nb[1] > 0 && m.nb[2] > 0 && (int64_t)m.nb[0] * m.nb[1] * m.nb[2] >= m.nmb,
+               MK_ERR_ARG, "mk_snapshot_build: block table too small");
+    MK_REQUIRE((m.n64 > 0) == (m.blocks64 != nullptr) && (m.blocks64 == nullptr) == (m.block64 == nullptr),
+               MK_ERR_ARG, "mk_snapshot_build: blocks64, block64 and n64 go together");
+    MK_REQUIRE(storage_bytes >= mk_snapshot_bytes(m.nmb, m.n), MK_ERR_ARG,
+               "mk_snapshot_build: storage of %zu bytes, need %zu", storage_bytes, mk_snapshot_bytes(m.nmb, m.n));
     MK_REQUIRE(((uintptr_t)storage_dev & 15) == 0, MK_ERR_ARG, "mk_snapshot_build: storage not 16-byte aligned");
-    const int64_t total = (int64_t)nmb * (n + 2) * (n + 2) * (n + 2);
+    const int64_t total = (int64_t)m.nmb * (m.n + 2) * (m.n + 2) * (m.n + 2);
     int64_t grid = (total + 255) / 256;
     const int64_t cap = (int64_t)device_sm_count() * 16;
     if (grid > cap) grid = cap;
-    snapshot_build_kernel<<<(unsigned)grid, 256, 0, as_stream(stream)>>>(uov_dev, B_dev, locs_dev, table_dev, nmb, n,
-                                                                       nb[0], nb[1], nb[2], (float *)storage_dev);
+    snapshot_build_kernel<<<(unsigned)grid, 256, 0, as_stream(stream)>>>(m, (float *)storage_dev);
     MK_LAUNCHED("snapshot_build_kernel");
-    float *gf = (float *)((char *)storage_dev + blocks_bytes(nmb, n));
-    geom_f32_kernel<<<grid_for(nmb, 128), 128, 0, as_stream(stream)>>>(geom_dev, nmb, gf);
+    float *gf = (float *)((char *)storage_dev + blocks_bytes(m.nmb, m.n));
+    geom_f32_kernel<<<grid_for(m.nmb, 128), 128, 0, as_stream(stream)>>>(m.geom, m.nmb, gf);
     MK_LAUNCHED("geom_f32_kernel");
     mk_snapshot_view v;
     v.blocks = (const float *)storage_dev;
-    v.geom = geom_dev;
+    v.geom = m.geom;
     v.geom_f32 = gf;
-    v.faces = faces_dev;
-    v.table = table_dev;
-    v.nmb = nmb;
-    v.n = n;
+    v.faces = m.faces;
+    v.table = m.table;
+    v.blocks64 = m.blocks64;
+    v.block64 = m.block64;
+    v.nmb = m.nmb;
+    v.n = m.n;
     v.pad0 = 0;
     for (int a = 0; a < 3; a++) {
-        v.nb[a] = nb[a];
-        v.lo[a] = lo[a];
-        v.width[a] = width[a];
+        v.nb[a] = m.nb[a];
+        v.lo[a] = m.lo[a];
+        v.width[a] = m.width[a];
     }
     *view_out = v;
     return MK_OK;

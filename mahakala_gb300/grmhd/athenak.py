@@ -7,9 +7,9 @@ GPU as ghost-filled AoS float32 meshblocks (built by ``mk_snapshot_build``);
 every sampling call runs in the sm_103a kernels.
 
 ``grmhd_filename`` may be a path to an ``.athdf`` file (needs h5py) or a
-``SnapshotArrays`` (the synthetic generator's output, or arrays the caller
-read itself).  Single-level meshes only: the multi-level ghost fill of
-athenak.py:235-502 is not built.
+``SnapshotArrays`` (the synthetic generators' output, or arrays the caller
+read itself).  Single- and multi-level meshes: the ghost fill of
+athenak.py:67-525 runs on the device (``mk_snapshot_build``).
 """
 
 import ctypes
@@ -41,8 +41,65 @@ def load_athdf(path):
                           VariableNames=tuple(names))
 
 
+def mesh_tables(arrs, max_table_cells=1 << 28):
+    """The block-grid metadata of a (single- or multi-level) mesh, from its
+    logical locations, levels and faces (no field data): the finest-level
+    block table, per-block faces, the sorted level/location keys, and which
+    blocks have a ghost region filled from finer neighbours (those get a
+    binary64 copy on the device)."""
+    locs = np.ascontiguousarray(np.asarray(arrs.LogicalLocations, dtype=np.int32))
+    levels = np.ascontiguousarray(np.asarray(arrs.Levels, dtype=np.int32))
+    nmb = len(levels)
+    if np.any(locs < 0) or np.any(levels < 0) or np.any(locs >= 1 << 18) or np.any(levels >= 512):
+        raise ValueError("logical locations must lie in [0, 2^18) and levels in [0, 512)")
+    keys = _lib.mesh_key(levels, locs[:, 0], locs[:, 1], locs[:, 2])
+    if len(np.unique(keys)) != nmb:
+        raise ValueError("duplicate (level, logical location) blocks")
+    order = np.argsort(keys, kind="stable")
+    faces = np.stack([arrs.x1f[:, 0], arrs.x1f[:, -1], arrs.x2f[:, 0], arrs.x2f[:, -1],
+                      arrs.x3f[:, 0], arrs.x3f[:, -1]], axis=1).astype(np.float64)
+    left, right = faces[:, 0::2], faces[:, 1::2]
+    widths = right - left
+    if np.any(widths <= 0):
+        raise ValueError("block faces must increase")
+    wf = widths.min(axis=0)
+    lo, hi = left.min(axis=0), right.max(axis=0)
+    nb = [int(round((hi[a] - lo[a]) / wf[a])) for a in range(3)]
+    if int(np.prod(nb, dtype=np.int64)) > max_table_cells:
+        raise ValueError(f"finest-level block table {nb} exceeds {max_table_cells} cells")
+    table = -np.ones((nb[2], nb[1], nb[0]), np.int32)
+    start = np.rint((left - lo) / wf).astype(np.int64)
+    span = np.rint(widths / wf).astype(np.int64)
+    for m in range(nmb):
+        sl = tuple(slice(start[m, a], start[m, a] + span[m, a]) for a in (2, 1, 0))
+        if np.any(table[sl] >= 0):
+            raise ValueError("overlapping blocks")
+        table[sl] = m
+    keyset = set(keys.tolist())
+    fine_ghosts = np.zeros(nmb, bool)
+    if np.any(levels != levels[0]):
+        for m in range(nmb):
+            lv, t = int(levels[m]), [int(v) for v in locs[m]]
+            for d in ((di, dj, dk) for di in (-1, 0, 1) for dj in (-1, 0, 1) for dk in (-1, 0, 1)):
+                if d == (0, 0, 0):
+                    continue
+                u = [t[a] + d[a] for a in range(3)]
+                if min(u) >= 0 and int(_lib.mesh_key(lv, *u)) in keyset:
+                    continue
+                if lv > 0 and int(_lib.mesh_key(lv - 1, *[v // 2 for v in u])) in keyset:
+                    continue
+                if min(u) >= 0 and int(_lib.mesh_key(lv + 1, *[2 * v for v in u])) in keyset:
+                    fine_ghosts[m] = True
+                    break
+    block64 = np.where(fine_ghosts, np.cumsum(fine_ghosts) - 1, -1).astype(np.int32)
+    return dict(locs=locs, levels=levels, keys=np.ascontiguousarray(keys[order]),
+                key_block=np.ascontiguousarray(order.astype(np.int32)), faces=faces, table=table, nb=nb,
+                lo=lo, width=wf, block64=block64, n64=int(fine_ghosts.sum()))
+
+
 class DeviceSnapshot:
-    """Resident meshblocks on one GPU plus the geometry tables of the lookup."""
+    """Resident meshblocks on one GPU plus the geometry tables of the lookup
+    (single- or multi-level meshes)."""
 
     def __init__(self, arrs, dev=None):
         dev = dev or device()
@@ -55,53 +112,50 @@ class DeviceSnapshot:
         nprim, nmb, nk, nj, ni = uov.shape
         if nprim != 5 or B.shape[0] != 3 or not (nk == nj == ni):
             raise ValueError("expected uov (5, nmb, n, n, n) and B (3, nmb, n, n, n) with cubic blocks")
-        levels = np.asarray(arrs.Levels)
-        if np.any(levels != levels[0]):
-            raise NotImplementedError("multi-level (AMR) snapshots are not supported yet")
         n = int(ni)
-        locs = np.ascontiguousarray(np.asarray(arrs.LogicalLocations, dtype=np.int32))
-        nb = [int(locs[:, c].max()) + 1 for c in range(3)]
-        if np.any(locs < 0):
-            raise ValueError("negative logical locations")
-        table = -np.ones((nb[2], nb[1], nb[0]), np.int32)
-        table[locs[:, 2], locs[:, 1], locs[:, 0]] = np.arange(nmb, dtype=np.int32)
-        if len(np.unique(locs, axis=0)) != nmb:
-            raise ValueError("duplicate logical locations")
-        faces = []
-        for c, f in enumerate((arrs.x1f, arrs.x2f, arrs.x3f)):
-            fa = np.full(nb[c] + 1, np.nan)
-            fa[locs[:, c]] = f[:, 0]
-            fa[locs[:, c] + 1] = f[:, -1]
-            if np.any(np.isnan(fa)) or np.any(np.diff(fa) <= 0):
-                raise ValueError("block faces do not form a single-level grid")
-            faces.append(fa)
+        t = mesh_tables(arrs)
         geom = np.stack([arrs.x1v[:, 0], arrs.x2v[:, 0], arrs.x3v[:, 0], arrs.x1v[:, 1] - arrs.x1v[:, 0],
                          arrs.x2v[:, 1] - arrs.x2v[:, 0], arrs.x3v[:, 1] - arrs.x3v[:, 0]], axis=1)
-        self.n, self.nmb, self.nb = n, nmb, nb
+        self.n, self.nmb, self.nb = n, nmb, t["nb"]
+        self.levels_host = t["levels"]
         self.device = dev
         self.geom = f64(geom, dev)
-        self.faces = f64(np.concatenate(faces), dev)
-        self.table = torch.as_tensor(table, device=dev)
-        self.locs = torch.as_tensor(locs, device=dev)
+        self.faces = f64(t["faces"], dev)
+        self.table = torch.as_tensor(t["table"], device=dev)
+        self.locs = torch.as_tensor(t["locs"], device=dev)
+        self.levels = torch.as_tensor(t["levels"], device=dev)
+        keys = torch.as_tensor(t["keys"], device=dev)
+        key_block = torch.as_tensor(t["key_block"], device=dev)
+        self.n64 = t["n64"]
+        n2 = n + 2
+        self.blocks64 = (torch.empty((self.n64, n2, n2, n2, 8), dtype=torch.float64, device=dev)
+                         if self.n64 else None)
+        self.block64 = torch.as_tensor(t["block64"], device=dev) if self.n64 else None
         nbytes = _lib.load().mk_snapshot_bytes(nmb, n)
         self.storage = torch.empty(nbytes // 4, dtype=torch.float32, device=dev)
         uov_d = torch.as_tensor(np.ascontiguousarray(uov, dtype=np.float32), device=dev)
         B_d = torch.as_tensor(np.ascontiguousarray(B, dtype=np.float32), device=dev)
-        lo = [float(fa[0]) for fa in faces]
-        width = [float((fa[-1] - fa[0]) / (len(fa) - 1)) for fa in faces]
+        mesh = _lib.MeshDesc()
+        mesh.uov, mesh.B, mesh.locs, mesh.levels = ptr(uov_d), ptr(B_d), ptr(self.locs), ptr(self.levels)
+        mesh.keys, mesh.key_block = ptr(keys), ptr(key_block)
+        mesh.geom, mesh.faces, mesh.table = ptr(self.geom), ptr(self.faces), ptr(self.table)
+        mesh.blocks64, mesh.block64 = ptr(self.blocks64), ptr(self.block64)
+        mesh.nmb, mesh.n, mesh.n64 = nmb, n, self.n64
+        for a in range(3):
+            mesh.nb[a], mesh.lo[a], mesh.width[a] = t["nb"][a], float(t["lo"][a]), float(t["width"][a])
         view = _lib.SnapshotView()
-        _lib.call("mk_snapshot_build", ptr(uov_d), ptr(B_d), ptr(self.locs), ptr(self.geom), ptr(self.faces),
-                  ptr(self.table), nmb, n, (ctypes.c_int32 * 3)(*nb), (ctypes.c_double * 3)(*lo),
-                  (ctypes.c_double * 3)(*width), ptr(self.storage), nbytes, ctypes.byref(view), stream_ptr())
+        _lib.call("mk_snapshot_build", ctypes.byref(mesh), ptr(self.storage), nbytes, ctypes.byref(view),
+                  stream_ptr())
         torch.cuda.current_stream().synchronize()
-        del uov_d, B_d
+        del uov_d, B_d, keys, key_block
         self.view = view
         self.view_dev = torch.frombuffer(bytearray(bytes(view)), dtype=torch.uint8).to(dev)
 
     @property
     def nbytes(self):
+        extra = self.blocks64.numel() * 8 + self.block64.numel() * 4 if self.n64 else 0
         return (self.storage.numel() * 4 + self.geom.numel() * 8 + self.faces.numel() * 8
-                + self.table.numel() * 4 + self.locs.numel() * 4)
+                + self.table.numel() * 4 + self.locs.numel() * 4 + self.levels.numel() * 4 + extra)
 
     def blocks(self):
         """(nmb, n+2, n+2, n+2, 8) float32 view of the resident meshblocks."""

@@ -36,7 +36,8 @@ def test_trim_rule_on_reference_fixture():
 def test_request_struct_layout():
     from mahakala_gb300 import _lib
     assert ctypes.sizeof(_lib.Request) == 304
-    assert ctypes.sizeof(_lib.SnapshotView) == 112
+    assert ctypes.sizeof(_lib.SnapshotView) == 128
+    assert ctypes.sizeof(_lib.MeshDesc) == 168
     assert _lib.Request.ray_offset.offset == 264
     assert _lib.Request.rows.offset == 296
 
@@ -130,3 +131,26 @@ def test_replicas_over_gloo():
     for rank, full, t in res:
         assert full == [10.0 * i for i in range(11)]
         assert t == 2.0
+
+
+@pytest.mark.parametrize("case", [0, 1])
+def test_mesh_tables_multilevel(case):
+    """Finest-level block table covers the refined mesh once per cell, each
+    block over exactly its own span; the blocks flagged for a binary64 copy
+    include every block whose reference ghost fill produced a value that is
+    not a float32 value (a fine-to-coarse mean)."""
+    from conftest import amr_arrays, golden
+    from mahakala_gb300.grmhd.athenak import mesh_tables
+    arrs = amr_arrays(case)
+    t = mesh_tables(arrs)
+    table = t["table"]
+    assert (table >= 0).all()
+    lv = np.asarray(arrs.Levels)
+    counts = np.bincount(table.ravel(), minlength=len(lv))
+    assert np.array_equal(counts, 8 ** (lv.max() - lv))      # a level-l block spans 2^(L-l) cells per axis
+    ref = golden("amr")[f"case{case}_all_meshblocks"]
+    inexact = np.any((ref.astype(np.float32).astype(np.float64) != ref).reshape(len(lv), -1), axis=1)
+    assert np.all(t["block64"][inexact] >= 0)
+    assert t["n64"] == int((t["block64"] >= 0).sum())
+    keys = t["keys"]
+    assert np.all(np.diff(keys) > 0)
