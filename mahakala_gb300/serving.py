@@ -213,10 +213,13 @@ class Scheduler:
                 time.sleep(sleep)
 
 
-def serve_stream(scheduler, arrivals, requests, sleep=1e-4):
+def serve_stream(scheduler, arrivals, requests, sleep=1e-4, poll=5e-5):
     """Feed requests at their arrival offsets (seconds from now) in real
-    time and run the scheduler until every request is finished.  Returns
-    the tickets and the wall time."""
+    time and run the scheduler until every request is finished.  While a
+    batch is in flight the loop polls every ``poll`` seconds (a finished
+    batch is collected within that time); with nothing in flight it sleeps
+    until the next arrival (at most 2 ms).  Returns the tickets and the
+    wall time."""
     order = np.argsort(arrivals)
     t0 = scheduler.clock()
     tickets = [None] * len(requests)
@@ -229,8 +232,20 @@ def serve_stream(scheduler, arrivals, requests, sleep=1e-4):
             i += 1
         if not scheduler.step():
             nxt = t0 + arrivals[order[i]] - scheduler.clock() if i < len(order) else sleep
-            time.sleep(min(max(nxt, 0.0), 2e-3) if nxt > 0 else sleep)
+            cap = poll if any(x is not None for x in scheduler.slots) else 2e-3
+            time.sleep(min(max(nxt, 0.0), cap) if nxt > 0 else min(sleep, cap))
     return tickets, scheduler.clock() - t0
+
+
+def isolated_latencies(scheduler_factory, requests):
+    """Arrival-to-host latency of each request served ALONE through a fresh
+    scheduler (same executor path: graph replay, copies, polling), in s."""
+    out = []
+    for r in requests:
+        sched = scheduler_factory()
+        tickets, _ = serve_stream(sched, np.zeros(1), [r])
+        out.append(tickets[0].latency)
+    return out
 
 
 def latency_report(tickets, wall, isolated=None):
