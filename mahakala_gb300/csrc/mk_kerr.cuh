@@ -58,6 +58,15 @@ __host__ __device__ constexpr dd sixth<dd>() { return dd(0x1.555556p-3f, -0x1.55
 // exact small constants in the arithmetic code are written as float
 // literals (0.5f, 2.0f, ...): the same value in double, float and pairs
 
+// Quotient for each arithmetic: binary64 and pairs divide exactly; the float
+// (mixed-form) paths take the hardware reciprocal (__fdividef: ~2 ulp, two
+// instructions instead of a division subroutine; |y| stays far below 2^126
+// here -- the largest divisor, (r^4 + a^2 z^2)(r^2 + a^2) at the camera, is
+// ~1e18).
+__device__ __forceinline__ float fdiv(float x, float y) { return __fdividef(x, y); }
+__device__ __forceinline__ double fdiv(double x, double y) { return x / y; }
+__device__ __forceinline__ dd fdiv(dd x, dd y) { return x / y; }
+
 // Kerr-Schild metric data at a point: g = eta + f l l
 template <typename T>
 struct KerrPoint {
@@ -100,7 +109,7 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
     const T den = rr * rr + aa * zz;
     const T rra = rr + aa;
     // one division for the two reciprocals 1/den and 1/(rr + a^2)
-    const T inv2 = T(1.0f) / (den * rra);
+    const T inv2 = fdiv(T(1.0f), den * rra);
     const T iden = rra * inv2;
     const T ira = den * inv2;
 
@@ -317,7 +326,7 @@ __host__ __device__ __forceinline__ double radius_eh(double a) { return 1.0 + sq
 // dt rule of geodesic_step (geodesics.py:249-252); why = stop reason
 template <typename T>
 __device__ __forceinline__ T reference_dt(T r, T r_eh, T div, T tol, int &why) {
-    const T dt = -(r - r_eh) / div;
+    const T dt = -fdiv(r - r_eh, div);
     why = MK_RAY_ACTIVE;
     if (isnan(dt)) { why = MK_RAY_NAN; return T(0); }
     const T adiv = fabs(dt) * div;
