@@ -545,8 +545,9 @@ def main():
         steps_total, samples_total = prep.work_totals()
         split = prep.precision_split() if form.startswith("mixed") else (0, 0, steps_total)
         samples64 = prep.samples_fp64() if form.startswith("mixed") else samples_total
+        work_b = prep.phase_b_work() if form == "mixed" else None
         res[form] = dict(prep=prep, req=req, t_step=t_step, t_phase=t_phase, steps=steps_total,
-                         zone_run_max=prep.zone_run_max() if form == "mixed" else None,
+                         zone_run_max=prep.zone_run_max() if form == "mixed" else None, work_b=work_b,
                          samples=samples_total, samples64=samples64,
                          split=split, image=prep.images[0].clone(), status=req.out["status"].clone(),
                          max_tau=prep.max_step_optical_depth())
@@ -587,16 +588,18 @@ def main():
                         r["t_phase"][0], peak64)]
         else:
             to64, back32, steps64 = r["split"]
-            f32 = (r["steps"] - steps64) * FLOP_PER_STEP + (r["samples"] - r["samples64"]) * per_sample
+            stb, smb = r["work_b"] if r["work_b"] else (steps64, r["samples64"])
+            f32 = (r["steps"] - stb) * FLOP_PER_STEP + (r["samples"] - smb) * per_sample
             # phase A does the FP32 steps up to the hand-off, phase C the rest;
             # their split is not counted, so both carry the FP32 total over their sum
-            tA, tB, tC = r["t_phase"]
-            zone = steps64 * FLOP_PER_STEP + r["samples64"] * per_sample
+            tA, tB, tC = (list(r["t_phase"]) + [0.0])[:3]   # MK_MIXED has no phase C
+            zone = stb * FLOP_PER_STEP + smb * per_sample
             if form == "mixed":  # float accelerations and emission, binary64 state and sums
-                kb = ("render_zone_kernel (phase B, near the hole)", "fp32", zone, tB, peak32)
+                kb = ("render_zone_kernel (phase B: near the hole and after)", "fp32", zone, tB, peak32)
             else:
                 kb = ("render_fp64_kernel (phase B, near the hole)", "fp64", zone, tB, peak64)
-            kernels = [("render_f32_kernel (phases A+C)", "fp32", f32, tA + tC, peak32), kb]
+            ka = "render_f32_kernel (phase A)" if form == "mixed" else "render_f32_kernel (phases A+C)"
+            kernels = [(ka, "fp32", f32, tA + tC, peak32), kb]
         table = [{"kernel": k, "bound": b, "flop": fl, "ms": 1e3 * t, "achieved": fl / t / 1e12 if t else None,
                   "peak": pk / 1e12, "frac": fl / t / pk if t else None} for k, b, fl, t, pk in kernels]
         top = max(table, key=lambda e: e["ms"])
@@ -671,7 +674,7 @@ def main():
                 "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
         "serving": serving,
         "sampling_stage": sampling,
-        "gpu_launches": args.steps * (1 if head == "fp64" else 3),
+        "gpu_launches": args.steps * {"fp64": 1, "mixed": 2}.get(head, 3),
         "phase_ms": {f: [1e3 * t for t in res[f]["t_phase"]] for f in forms},
         "clocks": clocks,
         "snapshot_build_s": t_gen,

@@ -272,7 +272,9 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
    explicit Euler update is stable below 1), MK_WS_TO_FP64 rays handed to
    FP64, MK_WS_STEPS_FP64 steps and MK_WS_SAMPLES_FP64 in-snapshot samples
    taken in FP64 (mixed form), MK_WS_ZONE_RUN_MAX the most steps one ray
-   took in one visit to the near-hole phase (MK_MIXED; its serial chain). */
+   took in one visit to the near-hole phase (MK_MIXED; its serial chain),
+   MK_WS_STEPS_B / MK_WS_SAMPLES_B the steps and samples MK_MIXED's second
+   launch took (near the hole and after). */
 #define MK_WS_STEPS 1
 #define MK_WS_SAMPLES 2
 #define MK_WS_MAX_TAU 3
@@ -281,6 +283,8 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
 #define MK_WS_STEPS_FP64 8
 #define MK_WS_SAMPLES_FP64 10
 #define MK_WS_ZONE_RUN_MAX 11
+#define MK_WS_STEPS_B 12
+#define MK_WS_SAMPLES_B 13
 size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision);
 
 /* make_image (images.py:30-144) for nreq requests in ONE persistent launch
@@ -343,8 +347,9 @@ int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_ra
 int mk_set_tuning(const char *name, int64_t value);
 
 /* Durations (ms) of the kernels of the last render launched with the
-   "phase_events" tuning set, on the current device: one for MK_FP64, three
-   (phases A, B, C) for the mixed forms; *nphases receives the count.
+   "phase_events" tuning set, on the current device: one for MK_FP64, two
+   (phases A, B) for MK_MIXED, three (A, B, C) for MK_MIXED_STRICT and
+   MK_MIXED_DF; *nphases receives the count.
    Waits for that render to finish.  No reference counterpart. */
 int mk_render_phase_ms(float *ms_out, int32_t *nphases);
 

@@ -29,6 +29,7 @@ NOALLOC_MAX_MIXED_RAYS = (NOALLOC_WORKSPACE_BYTES - 256) // 320
 MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_TO_FP32, MK_WS_STEPS_FP64 = 1, 2, 3, 4, 6, 8
 MK_WS_SAMPLES_FP64 = 10
 MK_WS_ZONE_RUN_MAX = 11
+MK_WS_STEPS_B, MK_WS_SAMPLES_B = 12, 13
 
 
 class MKError(RuntimeError):

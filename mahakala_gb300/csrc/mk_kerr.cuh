@@ -289,10 +289,12 @@ __device__ __forceinline__ void rk4_step_pair(const f2 X[4], const f2 K[4], cons
 
 // The RK4 increments of one step in float, for a state held elsewhere in
 // higher precision: x, k the state rounded to float, a1 the acceleration
-// there.  dX = dt k + dt^2/6 (a1 + a2 + a3), dK = dt/6 (a1 + 2 a2 + 2 a3 + a4)
-// -- RK4_gen's combination (geodesics.py:317-336) written for x'' = a(x, x').
+// there.  The position increment is dt k + dXa with dXa = dt^2/6 (a1 + a2 +
+// a3) (the caller forms dt k in its own precision), dK = dt/6 (a1 + 2 a2 +
+// 2 a3 + a4) -- RK4_gen's combination (geodesics.py:317-336) written for
+// x'' = a(x, x').
 __device__ __forceinline__ void rk4_increment_f32(const float x[4], const float k[4], const float a1[4], float dt,
-                                                  float a, float dX[4], float dK[4]) {
+                                                  float a, float dXa[4], float dK[4]) {
     float t[8], a2[4], a3[4], a4[4];
     const float h = 0.5f * dt;
 #pragma unroll
@@ -308,7 +310,7 @@ __device__ __forceinline__ void rk4_increment_f32(const float x[4], const float 
     const float d = dt * (1.0f / 6.0f);
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        dX[i] = dt * k[i] + c * (a1[i] + a2[i] + a3[i]);
+        dXa[i] = c * (a1[i] + a2[i] + a3[i]);
         dK[i] = d * (a1[i] + 2.0f * a2[i] + 2.0f * a3[i] + a4[i]);
     }
 }

@@ -20,17 +20,17 @@
 //
 // Precision forms:
 //   MK_FP64  one launch, every operation in FP64 (the reference's x64).
-//   MK_MIXED three launches on the caller's stream:
+//   MK_MIXED two launches on the caller's stream:
 //     A  FP32 from the camera.  A ray whose radius drops below R_FP64 (3 M),
 //        or that moves inward inside R_TURN (6 M, where photon-ring rays
 //        reach their turning points), is handed to a queue (FP64 record);
-//     B  that queue, the near-horizon steps and the turning points, with
-//        the state in binary64 (render_zone_kernel): renormalised to null
-//        in binary64 on entry and at each radial turning point.  A ray
-//        that leaves R_TURN outward is handed to a second queue;
-//     C  FP32 over the second queue until the ray stops.
-//   MK_MIXED_STRICT: phase B integrates the geodesic entirely in binary64
-//   (render_fp64_kernel over the queue); MK_MIXED_DF: the same in
+//     B  that queue (render_zone_kernel): near the hole the state is
+//        binary64, renormalised to null in binary64 on entry and at each
+//        radial turning point; a ray leaving R_TURN outward is renormalised
+//        once more and continues to its end on a float-pair state.
+//   MK_MIXED_STRICT: phase B integrates the near-hole geodesic entirely in
+//   binary64 (render_fp64_kernel over the queue) and parks rays leaving it
+//   for a third launch (phase C, FP32); MK_MIXED_DF: the same in
 //   double-float pairs.
 //   Splitting by precision keeps each warp uniform: on a part whose FP64
 //   rate is 1/64 of FP32, one FP64 lane would stall the other 31.  The
@@ -97,6 +97,8 @@ struct RenderWorkspace {
     unsigned long long overflow;      // queue overflow (cannot happen: capacity = rays)
     unsigned long long samples_fp64;  // in-snapshot samples taken in the FP64 phase (mixed form)
     unsigned long long zone_run_max;  // most steps one ray took in one visit to the near-hole phase
+    unsigned long long steps_b;       // all steps render_zone_kernel took (near the hole and after)
+    unsigned long long samples_b;     // all samples render_zone_kernel took
 };
 constexpr size_t WS_HEADER = 256;
 static_assert(sizeof(RenderWorkspace) <= WS_HEADER, "workspace header");
@@ -541,13 +543,12 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
 // meet at one named barrier per step (both warps execute it once per
 // iteration; the integrator's last message carries ZM_DONE and both leave
 // after that barrier).  No wait depends on another block.
-enum : unsigned { ZM_START = 1u, ZM_SAMPLE = 2u, ZM_END = 4u, ZM_PARK = 8u, ZM_DONE = 16u };
+enum : unsigned { ZM_START = 1u, ZM_SAMPLE = 2u, ZM_END = 4u, ZM_DONE = 16u, ZM_ZONE = 32u };
 constexpr int ZONE_THREADS = 64;
 
 struct ZoneMsgs {
     unsigned flags[2][32];
     int idx[2][32];   // ZM_START: index in the near-hole queue
-    int slot[2][32];  // ZM_PARK: slot in the second queue (a ray can start and park in one step)
     int steps[2][32];
     int why[2][32];
     float s[2][8][32];  // state after the step
@@ -565,15 +566,21 @@ __device__ __forceinline__ void zone_barrier() {
 
 __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ reqs,
                                                const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws,
-                                               RayRecord *q64, RayRecord *q32, long long capacity, ZoneMsgs &msg) {
+                                               const RayRecord *q64, long long capacity, ZoneMsgs &msg) {
     const int lane = threadIdx.x & 31;
     unsigned long long *counter = &ws->q64_next;
     const long long total = min((long long)*(volatile unsigned long long *)&ws->q64_count, capacity);
     bool active = false, exhausted = false;
-    int rq = 0, steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0;
+    int rq = 0, steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0, b_steps = 0;
     long long ray = 0;
+    // near the hole: binary64 state s; after the ray leaves it outward the
+    // integration continues here on a float-pair state (X, K) as in the
+    // FP32 phases (the ray's remaining ~250 steps would otherwise wait for a
+    // third launch)
+    bool inzone = true;
     double s[8], bhspin = 0.0;
-    float xf[8];  // s rounded to float
+    f2 X[4], K[4];
+    float xf[8];  // the state rounded to float
     float d1[4], dt = 0.0f, r_cur = 0.0f, dr_prev = 0.0f, reh = 0.0f, a = 0.0f, div = 0.0f, tol = 0.0f;
     SnapF32 sf;
 
@@ -605,6 +612,7 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             r_cur = m.r;
             dr_prev = 0.0f;
             run = 0;
+            inzone = true;
             flags |= ZM_START;
             msg.idx[b][lane] = (int)idx;
             int why = MK_RAY_ACTIVE;
@@ -619,14 +627,28 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
         }
         const bool any = __any_sync(0xffffffffu, active);
         if (active) {
-            float dX[4], dK[4];
-            rk4_increment_f32(xf, xf + 4, d1, dt, a, dX, dK);
+            float xa[4], dK[4];
+            rk4_increment_f32(xf, xf + 4, d1, dt, a, xa, dK);
             double sn[8];
-#pragma unroll
-            for (int i = 0; i < 4; i++) { sn[i] = s[i] + (double)dX[i]; sn[4 + i] = s[4 + i] + (double)dK[i]; }
+            f2 Xn[4], Kn[4];
             float xn[8];
+            if (inzone) {
 #pragma unroll
-            for (int i = 0; i < 8; i++) xn[i] = (float)sn[i];
+                for (int i = 0; i < 4; i++) {
+                    sn[i] = s[i] + (double)(dt * xf[4 + i] + xa[i]);
+                    sn[4 + i] = s[4 + i] + (double)dK[i];
+                }
+#pragma unroll
+                for (int i = 0; i < 8; i++) xn[i] = (float)sn[i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    Xn[i] = f2_add(X[i], f2_add(f2_mul(K[i], dt), xa[i]));
+                    Kn[i] = f2_add(K[i], dK[i]);
+                    xn[i] = Xn[i].hi;
+                    xn[4 + i] = Kn[i].hi;
+                }
+            }
             const mk_snapshot_view &sv = snaps[reqs[rq].snapshot];
             CellPosF cell;
             const bool inside = locate_f32(sv, sf, xn[1], xn[2], xn[3], cell);
@@ -644,11 +666,18 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                 msg.steps[b][lane] = steps;
                 active = false;
             } else {
+                if (inzone) {
 #pragma unroll
-                for (int i = 0; i < 8; i++) { s[i] = sn[i]; xf[i] = xn[i]; }
+                    for (int i = 0; i < 8; i++) s[i] = sn[i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) { X[i] = Xn[i]; K[i] = Kn[i]; }
+                }
+#pragma unroll
+                for (int i = 0; i < 8; i++) xf[i] = xn[i];
 #pragma unroll
                 for (int i = 0; i < 4; i++) d1[i] = dn[i];
-                flags |= ZM_SAMPLE;
+                flags |= ZM_SAMPLE | (inzone ? ZM_ZONE : 0u);
 #pragma unroll
                 for (int i = 0; i < 8; i++) msg.s[b][i][lane] = xn[i];
                 msg.m[b][0][lane] = m.r;
@@ -662,8 +691,11 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                 for (int i = 0; i < 3; i++) { msg.cidx[b][i][lane] = cell.idx[i]; msg.cdel[b][i][lane] = cell.del[i]; }
                 dt = dtn;
                 ++steps;
-                ++zone_steps;
-                run_max = max(run_max, ++run);
+                ++b_steps;
+                if (inzone) {
+                    ++zone_steps;
+                    run_max = max(run_max, ++run);
+                }
                 const float dr = r_new - r_cur;
                 if (steps >= nmax - 1) {
                     // trajectory rows stop at N-1: step N-1 never reaches the solve
@@ -671,23 +703,21 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                     msg.why[b][lane] = MK_RAY_MAXSTEPS;
                     msg.steps[b][lane] = steps;
                     active = false;
-                } else if (r_new >= (float)R_TURN && dr > 0.0f) {
-                    // outbound past the photon-ring region: back to FP32
-                    const unsigned long long slot = atomicAdd(&ws->q32_count, 1ull);
-                    if ((long long)slot < capacity) {
-                        RayRecord &q = q32[slot];
+                } else if (inzone && r_new >= (float)R_TURN && dr > 0.0f) {
+                    // outbound past the photon-ring region: renormalise to null in
+                    // binary64 and continue on a float-pair state
+                    renull_fp64(s, bhspin);
 #pragma unroll
-                        for (int i = 0; i < 8; i++) q.s[i] = s[i];
-                        q.ray = ray;
-                        q.steps = steps;
-                        q.rq = rq;
-                        flags |= ZM_PARK;
-                        msg.slot[b][lane] = (int)slot;
-                        active = false;
-                    } else {
-                        atomicAdd(&ws->overflow, 1ull);  // keep integrating here
+                    for (int i = 0; i < 4; i++) {
+                        X[i] = f2_from(s[i]);
+                        K[i] = f2_from(s[4 + i]);
+                        xf[i] = X[i].hi;
+                        xf[4 + i] = K[i].hi;
                     }
-                } else if ((dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f)) {
+                    kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3]);
+                    inzone = false;
+                    atomicAdd(&ws->q32_count, 1ull);  // counted as a ray back in FP32
+                } else if (inzone && ((dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f))) {
                     // radial turning point: renormalise to null in binary64 and
                     // re-evaluate the first stage of the next step there
                     renull_fp64(s, bhspin);
@@ -703,14 +733,15 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
         if (!any) break;
     }
     if (zone_steps) atomicAdd(&ws->steps_fp64, (unsigned long long)zone_steps);
+    if (b_steps) atomicAdd(&ws->steps_b, (unsigned long long)b_steps);
     if (run_max) atomicMax(&ws->zone_run_max, (unsigned long long)run_max);
 }
 
 __device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
                                             const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws,
-                                            const RayRecord *q64, RayRecord *q32, const ZoneMsgs &msg) {
+                                            const RayRecord *q64, const ZoneMsgs &msg) {
     const int lane = threadIdx.x & 31;
-    int rq = 0, nsamples = 0, zone_samples = 0;
+    int rq = 0, nsamples = 0, zone_samples = 0, b_samples = 0;
     int64_t pix = 0;
     double I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0, L_unit = 0.0;
     SynchroF32 sc[MK_MAX_NU];
@@ -750,30 +781,24 @@ __device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
             m.l3 = msg.m[b][4][lane];
             sample_f32_sum64(snaps[reqs[rq].snapshot], c, rc, x, m, -(double)msg.dt[b][lane] * L_unit, I, P, sc,
                              nsamples, max_tau);
-            ++zone_samples;
+            if (flags & ZM_ZONE) ++zone_samples;
+            ++b_samples;
         }
-        if (flags & ZM_END) {
-            finish_ray(reqs[rq], pix, I, msg.steps[b][lane], msg.why[b][lane], nsamples, max_tau, ws);
-        } else if (flags & ZM_PARK) {
-            RayRecord &q = q32[msg.slot[b][lane]];
-#pragma unroll
-            for (int ch = 0; ch < MK_MAX_NU; ch++) { q.I[ch] = I[ch]; q.P[ch] = P[ch]; }
-            q.max_tau = max_tau;
-            q.nsamples = nsamples;
-        }
+        if (flags & ZM_END) finish_ray(reqs[rq], pix, I, msg.steps[b][lane], msg.why[b][lane], nsamples, max_tau, ws);
         if (flags & ZM_DONE) break;
     }
     if (zone_samples) atomicAdd(&ws->samples_fp64, (unsigned long long)zone_samples);
+    if (b_samples) atomicAdd(&ws->samples_b, (unsigned long long)b_samples);
 }
 
 __global__ void __launch_bounds__(ZONE_THREADS)
 render_zone_kernel(const mk_request *__restrict__ reqs, const mk_snapshot_view *__restrict__ snaps,
-                   RenderWorkspace *ws, RayRecord *q64, RayRecord *q32, long long capacity) {
+                   RenderWorkspace *ws, const RayRecord *q64, long long capacity) {
     __shared__ ZoneMsgs msg;
     if (threadIdx.x < 32)
-        zone_integrate(reqs, snaps, ws, q64, q32, capacity, msg);
+        zone_integrate(reqs, snaps, ws, q64, capacity, msg);
     else
-        zone_sample(reqs, snaps, ws, q64, q32, msg);
+        zone_sample(reqs, snaps, ws, q64, msg);
 }
 
 __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix, const float I[MK_MAX_NU],
@@ -1011,16 +1036,18 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
                st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, g_fp64_zone);
     MK_LAUNCHED("render_f32_kernel (camera)");
     if ((rc = phase_mark(st, 1)) != MK_OK) return rc;
-    // The queues' sizes are only known on the device: persistent grids.
-    // Phase B runs one warp per block, 4 blocks per SM: the few FP64 rays
-    // spread over every SM sub-partition instead of queuing on the FP64
-    // units of a few SMs (one FP64 warp instruction occupies a
-    // sub-partition's FP64 unit for tens of cycles on this part).
+    // The queues' sizes are only known on the device: persistent grids,
+    // small blocks, so the few rays near the hole spread over every SM
+    // sub-partition (they are latency-bound: one FP64 warp instruction holds
+    // a sub-partition's FP64 unit for tens of cycles on this part).
     if (precision == MK_MIXED) {
+        // phase B carries its rays to their end: no phase C
         render_zone_kernel<<<(unsigned)device_sm_count() * 4, ZONE_THREADS, 0, st>>>(reqs_dev, snaps_dev, ws, q64,
-                                                                                      q32, cap);
+                                                                                      cap);
         MK_LAUNCHED("render_zone_kernel");
-    } else {
+        return phase_mark(st, 2);
+    }
+    {
         const int per_warp = g_fp64_rays_per_warp;
         const int stride = 32 / per_warp;
         const unsigned grid = (unsigned)device_sm_count() * (per_warp >= 32 ? 4 : 16);

@@ -157,6 +157,12 @@ class PreparedRender:
         mixed-form launch (syncs)."""
         return int(self.ws[:32].cpu()[_lib.MK_WS_SAMPLES_FP64])
 
+    def phase_b_work(self):
+        """(steps, samples) the last MK_MIXED launch's second kernel took
+        (syncs)."""
+        w = self.ws[:32].cpu()
+        return int(w[_lib.MK_WS_STEPS_B]), int(w[_lib.MK_WS_SAMPLES_B])
+
     def zone_run_max(self):
         """Most steps one ray took in one visit to the mixed form's
         near-hole phase in the last launch (syncs): that phase's serial
