@@ -633,13 +633,23 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             f2 Xn[4], Kn[4];
             float xn[8];
             if (inzone) {
+                // binary64 state; its float copy follows the float increments
+                // and is re-rounded from it every 8th step (a few float ulps of
+                // drift at most, below the float accelerations' own error; a
+                // binary64 -> float conversion per component and step held the
+                // integrating warp's issue for ~450 cycles)
+                float inc[8];
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    sn[i] = s[i] + (double)(dt * xf[4 + i] + xa[i]);
-                    sn[4 + i] = s[4 + i] + (double)dK[i];
+                for (int i = 0; i < 4; i++) { inc[i] = dt * xf[4 + i] + xa[i]; inc[4 + i] = dK[i]; }
+#pragma unroll
+                for (int i = 0; i < 8; i++) sn[i] = s[i] + (double)inc[i];
+                if ((run & 7) == 7) {
+#pragma unroll
+                    for (int i = 0; i < 8; i++) xn[i] = (float)sn[i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 8; i++) xn[i] = xf[i] + inc[i];
                 }
-#pragma unroll
-                for (int i = 0; i < 8; i++) xn[i] = (float)sn[i];
             } else {
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
