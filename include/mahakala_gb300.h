@@ -283,6 +283,10 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
 #define MK_WS_STEPS_FP64 8
 #define MK_WS_SAMPLES_FP64 10
 #define MK_WS_ZONE_RUN_MAX 11
+/* Requests one mixed-form launch takes (mk_render refuses more with
+   MK_ERR_LIMIT; rays of requests beyond it in an mk_render_job header end
+   with MK_RAY_NAN). */
+#define MK_MAX_REQUESTS_MIXED 128
 #define MK_WS_STEPS_B 12
 #define MK_WS_SAMPLES_B 13
 size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision);

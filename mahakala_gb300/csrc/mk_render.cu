@@ -365,6 +365,26 @@ __device__ __forceinline__ void sample_f32_at(const mk_request &R, const mk_snap
 
 enum { SRC_CAMERA = 0, SRC_QUEUE = 1 };
 
+// A request's float constants, one shared-memory entry per request of the
+// launch: read where used instead of held in ~37 registers per ray, which
+// lets the FP32 phases keep more warps resident.
+struct ReqF32 {
+    RayF32 rc;
+    SynchroF32 sc[MK_MAX_NU];
+    SnapF32 sf;
+    float a, reh;
+};
+
+__device__ __forceinline__ void fill_req_f32(const mk_request &R, const mk_snapshot_view *snaps, ReqF32 &o) {
+    o.rc = ray_f32(R);
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++)
+        if (ch < R.nnu) o.sc[ch] = synchro_consts(R.nu[ch]);
+    o.sf = snap_f32(snaps[R.snapshot]);
+    o.a = (float)R.camera.bhspin;
+    o.reh = (float)radius_eh(R.camera.bhspin);
+}
+
 
 
 // FP64 render.  SRC_CAMERA: every ray of the job, start to end (MK_FP64).
@@ -833,6 +853,9 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
         nreq = job->nreq;
         total_camera = job->total_rays;
     }
+    __shared__ ReqF32 s_req[MK_MAX_REQUESTS_MIXED];
+    for (int q = threadIdx.x; q < min(nreq, MK_MAX_REQUESTS_MIXED); q += blockDim.x) fill_req_f32(reqs[q], snaps, s_req[q]);
+    __syncthreads();
     unsigned long long *counter = SRC == SRC_CAMERA ? &ws->counter : &ws->q32_next;
     const long long total =
         SRC == SRC_CAMERA ? total_camera
@@ -842,11 +865,8 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
     long long ray = 0;
     int64_t pix = 0;
     f2 X[4], K[4];
-    float d1[4], dt = 0.0f, r_cur = 0.0f, reh = 0.0f, a = 0.0f, max_tau = 0.0f;
+    float d1[4], dt = 0.0f, r_cur = 0.0f, max_tau = 0.0f;
     float I[MK_MAX_NU], Ic[MK_MAX_NU], P[MK_MAX_NU];
-    SynchroF32 sc[MK_MAX_NU];
-    SnapF32 sf;
-    RayF32 rc;
 
     for (;;) {
         const long long idx = fetch(!active && !exhausted, counter, total);
@@ -881,43 +901,47 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 renull_fp64(s64, reqs[rq].camera.bhspin);
             }
             const mk_request &R = reqs[rq];
-#pragma unroll
-            for (int i = 0; i < 4; i++) { X[i] = f2_from(s64[i]); K[i] = f2_from(s64[4 + i]); }
-            a = (float)R.camera.bhspin;
-            reh = (float)radius_eh(R.camera.bhspin);
-#pragma unroll
-            for (int ch = 0; ch < MK_MAX_NU; ch++)
-                if (ch < R.nnu) sc[ch] = synchro_consts(R.nu[ch]);
-            sf = snap_f32(snaps[R.snapshot]);
-            rc = ray_f32(R);
-            KerrPoint<float> m;
-            kerr_accel(X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi, a, d1[0], d1[1], d1[2], d1[3],
-                       m);
-            r_cur = m.r;
-            dt = reference_dt(r_cur, reh, rc.div, rc.tol, why);
-            if (dt == 0.0f || R.policy.nmax < 2) {
-                if (why == MK_RAY_ACTIVE) why = MK_RAY_MAXSTEPS;
-                finish_ray_f32(R, pix, I, Ic, steps, why, nsamples, max_tau, ws);
+            if (rq >= MK_MAX_REQUESTS_MIXED) {  // beyond the launch's request table
+                atomicAdd(&ws->overflow, 1ull);
+                finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_NAN, nsamples, max_tau, ws);
             } else {
-                active = true;
+                const ReqF32 &Q = s_req[rq];
+#pragma unroll
+                for (int i = 0; i < 4; i++) { X[i] = f2_from(s64[i]); K[i] = f2_from(s64[4 + i]); }
+                KerrPoint<float> m;
+                kerr_accel(X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi, Q.a, d1[0], d1[1], d1[2],
+                           d1[3], m);
+                r_cur = m.r;
+                dt = reference_dt(r_cur, Q.reh, Q.rc.div, Q.rc.tol, why);
+                if (dt == 0.0f || R.policy.nmax < 2) {
+                    if (why == MK_RAY_ACTIVE) why = MK_RAY_MAXSTEPS;
+                    finish_ray_f32(R, pix, I, Ic, steps, why, nsamples, max_tau, ws);
+                } else {
+                    active = true;
+                }
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
             const mk_request &R = reqs[rq];
+            // re-read the request constants every step: an address the
+            // compiler cannot hoist keeps them out of the loop's registers
+            const ReqF32 *qp = s_req + rq;
+            asm volatile("" : "+l"(qp));
+            const ReqF32 &Q = *qp;
             f2 Xn[4], Kn[4];
             float dn[4];
-            rk4_step_pair(X, K, d1, dt, a, Xn, Kn);
+            rk4_step_pair(X, K, d1, dt, Q.a, Xn, Kn);
             const mk_snapshot_view &sv = snaps[R.snapshot];
             CellPosF cell;
-            const bool inside = locate_f32(sv, sf, Xn[1].hi, Xn[2].hi, Xn[3].hi, cell);
+            const bool inside = locate_f32(sv, Q.sf, Xn[1].hi, Xn[2].hi, Xn[3].hi, cell);
             if (inside) prefetch_cells_f32(sv, cell);
             KerrPoint<float> m;
-            kerr_accel(Xn[1].hi, Xn[2].hi, Xn[3].hi, Kn[0].hi, Kn[1].hi, Kn[2].hi, Kn[3].hi, a, dn[0], dn[1], dn[2],
-                       dn[3], m);
+            kerr_accel(Xn[1].hi, Xn[2].hi, Xn[3].hi, Kn[0].hi, Kn[1].hi, Kn[2].hi, Kn[3].hi, Q.a, dn[0], dn[1],
+                       dn[2], dn[3], m);
             int w1;
             const float r_new = m.r;
-            const float dtn = reference_dt(r_new, reh, rc.div, rc.tol, w1);
+            const float dtn = reference_dt(r_new, Q.reh, Q.rc.div, Q.rc.tol, w1);
             if (dtn == 0.0f) {
                 finish_ray_f32(R, pix, I, Ic, steps, w1, nsamples, max_tau, ws);
                 active = false;
@@ -928,7 +952,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 dt = dtn;
                 ++steps;
                 const float sh[8] = {X[0].hi, X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi};
-                if (inside) sample_f32(sv, cell, rc, sh, m, dt_used, I, Ic, P, sc, nsamples, max_tau);
+                if (inside) sample_f32(sv, cell, Q.rc, sh, m, dt_used, I, Ic, P, Q.sc, nsamples, max_tau);
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
                     active = false;
@@ -1094,6 +1118,8 @@ extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     const size_t need = mk_render_workspace_bytes(total_rays, precision);
     MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render: workspace of %zu bytes, need %zu",
                workspace_bytes, need);
+    MK_REQUIRE(precision == MK_FP64 || nreq <= MK_MAX_REQUESTS_MIXED, MK_ERR_LIMIT,
+               "mk_render: %d requests in one mixed-form launch, at most %d", (int)nreq, MK_MAX_REQUESTS_MIXED);
     MK_REQUIRE(((uintptr_t)workspace_dev & 15) == 0, MK_ERR_ARG, "mk_render: workspace not 16-byte aligned");
     return mk::launch_render(reqs_dev, nreq, total_rays, total_rays, nullptr, snaps_dev, precision, workspace_dev,
                              mk::as_stream(stream));
