@@ -342,9 +342,10 @@ int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_ra
    of the mixed form's FP64 phase carries.
    "fp64_zone" (0 or 1; default 1): 0 keeps every ray of the mixed forms in
    FP32 to its end, with no FP64 phase (measures what that phase buys).
-   "f32_blocks_per_sm" (3 or 4; default 4): the FP32 phases' kernels
-   compiled for 3 resident blocks per SM (no register spills) or 4
-   (registers capped at 128).
+   "f32_blocks_per_sm" (0, 3, 4 or 5; default 0): the FP32 phases' kernels
+   compiled for 3 resident blocks per SM (no register spills), 4 (128
+   registers) or 5 (96 registers); 0 takes 4 when the launch's rays fit one
+   wave of 4-block slots and 5 otherwise.
    "phase_events" (0 or 1; default 0): renders record CUDA events on their
    stream around each kernel for mk_render_phase_ms; not for renders that
    are captured into a CUDA graph. */

@@ -57,8 +57,10 @@ static int g_fp64_rays_per_warp = 32;
 // the FP64 region buys in accuracy)
 static int g_fp64_zone = 1;
 // resident blocks per SM the FP32 phases are compiled for: 3 (no register
-// spills) or 4 (registers capped at 128, a few spills)
-static int g_f32_blocks = 4;
+// spills), 4 (registers capped at 128, a few spills), 5 (96 registers, more
+// spills); 0 picks 4 when the launch's rays fit the GPU's 4-block slots in
+// one wave and 5 when they do not (more resident warps pay only then)
+static int g_f32_blocks = 0;
 // measurement switch: when set, each render records a CUDA event on its
 // stream before its first kernel and after each kernel, so the phases can
 // be timed apart (mk_render_phase_ms).  Process-wide, off by default; not
@@ -1017,7 +1019,8 @@ extern "C" int mk_set_tuning(const char *name, int64_t value) {
         return MK_OK;
     }
     if (!strcmp(name, "f32_blocks_per_sm")) {
-        MK_REQUIRE(value == 3 || value == 4, MK_ERR_ARG, "mk_set_tuning: f32_blocks_per_sm must be 3 or 4");
+        MK_REQUIRE(value == 0 || (value >= 3 && value <= 5), MK_ERR_ARG,
+                   "mk_set_tuning: f32_blocks_per_sm must be 0 (automatic), 3, 4 or 5");
         g_f32_blocks = (int)value;
         return MK_OK;
     }
@@ -1060,7 +1063,14 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     RayRecord *q64 = (RayRecord *)((char *)workspace_dev + WS_HEADER);
     RayRecord *q32 = q64 + max_rays;
     const long long cap = (long long)max_rays;
-    if (g_f32_blocks == 4)
+    int f32_blocks = g_f32_blocks;
+    if (f32_blocks == 0)
+        f32_blocks = max_rays > (int64_t)device_sm_count() * 4 * RENDER_THREADS ? 5 : 4;
+    if (f32_blocks == 5)
+        render_f32_kernel<SRC_CAMERA, 5>
+            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 5>, 5), max_rays), RENDER_THREADS, 0,
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, g_fp64_zone);
+    else if (f32_blocks == 4)
         render_f32_kernel<SRC_CAMERA, 4>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 4>, 1), max_rays), RENDER_THREADS, 0,
                st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, g_fp64_zone);
@@ -1094,7 +1104,7 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
         MK_LAUNCHED("render_fp64_kernel (queue)");
     }
     if ((rc = phase_mark(st, 2)) != MK_OK) return rc;
-    if (g_f32_blocks == 4)
+    if (f32_blocks >= 4)
         render_f32_kernel<SRC_QUEUE, 4>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 4>, 3), max_rays), RENDER_THREADS, 0,
                st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);

@@ -134,7 +134,9 @@ class PreparedRender:
         self.snaps_dev = torch.cat([sn.view_dev for sn in snaps]) if len(snaps) > 1 else snaps[0].view_dev
         self.nsnap = len(snaps)
         nbytes = _lib.load().mk_render_workspace_bytes(self.total_rays, self.precision)
-        self.ws = torch.zeros((nbytes + 7) // 8, dtype=torch.int64, device=dev)
+        # mk_render clears the counter header itself; the queue records are
+        # written before they are read
+        self.ws = torch.empty((nbytes + 7) // 8, dtype=torch.int64, device=dev)
 
     def launch(self, stream=None):
         _lib.call("mk_render", ptr(self.reqs_dev), len(self.requests), self.total_rays, ptr(self.snaps_dev),
