@@ -546,11 +546,20 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
     if (SRC == SRC_QUEUE && fp64_samples) atomicAdd(&ws->samples_fp64, (unsigned long long)fp64_samples);
 }
 
+__device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix, const float I[MK_MAX_NU],
+                                               const float Ic[MK_MAX_NU], int steps, int why, int nsamples,
+                                               float max_tau, RenderWorkspace *ws) {
+    double Iout[MK_MAX_NU];
+#pragma unroll
+    for (int ch = 0; ch < MK_MAX_NU; ch++) Iout[ch] = (double)I[ch] - (double)Ic[ch];
+    finish_ray(R, pix, Iout, steps, why, nsamples, (double)max_tau, ws);
+}
+
 // Mixed-form phase B (MK_MIXED): the rays near the hole.  The state is
 // held in binary64 and advanced by RK4 increments formed in float from the
 // state rounded to float (rk4_increment_f32); the wavevector is
 // renormalised to null in binary64 on entry and at every radial turning
-// point; the intensity and transmission sums are binary64.  The
+// point; the intensity and transmission sums are compensated floats.  The
 // accelerations and the emission are float, as in phases A and C: on this
 // part a binary64 acceleration costs ~33x a float one per step, and over
 // the measured images it changed the error against the FP64 form by less
@@ -602,6 +611,7 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
     bool inzone = true;
     double s[8], bhspin = 0.0;
     f2 X[4], K[4];
+    mk_snapshot_view sv;  // this ray's snapshot, loaded once
     float xf[8];  // the state rounded to float
     float d1[4], dt = 0.0f, r_cur = 0.0f, dr_prev = 0.0f, reh = 0.0f, a = 0.0f, div = 0.0f, tol = 0.0f;
     SnapF32 sf;
@@ -626,7 +636,8 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             renull_fp64(s, bhspin);
             a = (float)bhspin;
             reh = (float)radius_eh(bhspin);
-            sf = snap_f32(snaps[R.snapshot]);
+            sv = snaps[R.snapshot];
+            sf = snap_f32(sv);
 #pragma unroll
             for (int i = 0; i < 8; i++) xf[i] = (float)s[i];
             KerrPoint<float> m;
@@ -681,7 +692,6 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                     xn[4 + i] = Kn[i].hi;
                 }
             }
-            const mk_snapshot_view &sv = snaps[reqs[rq].snapshot];
             CellPosF cell;
             const bool inside = locate_f32(sv, sf, xn[1], xn[2], xn[3], cell);
             if (inside) prefetch_cells_f32(sv, cell);
@@ -775,9 +785,12 @@ __device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
     const int lane = threadIdx.x & 31;
     int rq = 0, nsamples = 0, zone_samples = 0, b_samples = 0;
     int64_t pix = 0;
-    double I[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0, L_unit = 0.0;
+    // Kahan-compensated float sums, as in phase A (binary64 sums cost this
+    // warp ~2.5 k cycles per sample on the chain's critical path)
+    float I[MK_MAX_NU], Ic[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0f;
     SynchroF32 sc[MK_MAX_NU];
     RayF32 rc;
+    mk_snapshot_view sv;  // this ray's snapshot, loaded once
     for (int it = 0;; ++it) {
         const int b = it & 1;
         zone_barrier();
@@ -785,14 +798,18 @@ __device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
         if (flags & ZM_START) {
             const RayRecord &q = q64[msg.idx[b][lane]];
 #pragma unroll
-            for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = q.I[ch]; P[ch] = q.P[ch]; }
-            max_tau = q.max_tau;
+            for (int ch = 0; ch < MK_MAX_NU; ch++) {
+                I[ch] = (float)q.I[ch];
+                Ic[ch] = (float)((double)I[ch] - q.I[ch]);
+                P[ch] = (float)q.P[ch];
+            }
+            max_tau = (float)q.max_tau;
             nsamples = q.nsamples;
             rq = q.rq;
             const mk_request &R = reqs[rq];
             pix = q.ray - R.ray_offset;
-            L_unit = R.L_unit;
             rc = ray_f32(R);
+            sv = snaps[R.snapshot];
 #pragma unroll
             for (int ch = 0; ch < MK_MAX_NU; ch++)
                 if (ch < R.nnu) sc[ch] = synchro_consts(R.nu[ch]);
@@ -811,12 +828,12 @@ __device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
             m.l1 = msg.m[b][2][lane];
             m.l2 = msg.m[b][3][lane];
             m.l3 = msg.m[b][4][lane];
-            sample_f32_sum64(snaps[reqs[rq].snapshot], c, rc, x, m, -(double)msg.dt[b][lane] * L_unit, I, P, sc,
-                             nsamples, max_tau);
+            sample_f32(sv, c, rc, x, m, msg.dt[b][lane], I, Ic, P, sc, nsamples, max_tau);
             if (flags & ZM_ZONE) ++zone_samples;
             ++b_samples;
         }
-        if (flags & ZM_END) finish_ray(reqs[rq], pix, I, msg.steps[b][lane], msg.why[b][lane], nsamples, max_tau, ws);
+        if (flags & ZM_END)
+            finish_ray_f32(reqs[rq], pix, I, Ic, msg.steps[b][lane], msg.why[b][lane], nsamples, max_tau, ws);
         if (flags & ZM_DONE) break;
     }
     if (zone_samples) atomicAdd(&ws->samples_fp64, (unsigned long long)zone_samples);
@@ -833,14 +850,6 @@ render_zone_kernel(const mk_request *__restrict__ reqs, const mk_snapshot_view *
         zone_sample(reqs, snaps, ws, q64, msg);
 }
 
-__device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix, const float I[MK_MAX_NU],
-                                               const float Ic[MK_MAX_NU], int steps, int why, int nsamples,
-                                               float max_tau, RenderWorkspace *ws) {
-    double Iout[MK_MAX_NU];
-#pragma unroll
-    for (int ch = 0; ch < MK_MAX_NU; ch++) Iout[ch] = (double)I[ch] - (double)Ic[ch];
-    finish_ray(R, pix, Iout, steps, why, nsamples, (double)max_tau, ws);
-}
 
 // FP32 render phase.  SRC_CAMERA: mixed-form phase A from the camera, with
 // hand-off to the FP64 queue.  SRC_QUEUE: phase C over the FP32 queue.
