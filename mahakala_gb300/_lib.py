@@ -30,6 +30,7 @@ MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_TO_FP32, MK_WS_S
 MK_WS_SAMPLES_FP64 = 10
 MK_WS_ZONE_RUN_MAX = 11
 MK_WS_STEPS_B, MK_WS_SAMPLES_B = 12, 13
+MK_MAX_REQUESTS_MIXED = 128
 
 
 class MKError(RuntimeError):

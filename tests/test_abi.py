@@ -46,7 +46,8 @@ def test_binding_covers_header(lib):
 def test_struct_layouts(lib):
     from mahakala_gb300 import _lib
     for name, cls in (("mk_step_policy", _lib.StepPolicy), ("mk_camera", _lib.Camera),
-                      ("mk_snapshot_view", _lib.SnapshotView), ("mk_request", _lib.Request)):
+                      ("mk_snapshot_view", _lib.SnapshotView), ("mk_mesh_desc", _lib.MeshDesc),
+                      ("mk_request", _lib.Request)):
         assert lib.mk_sizeof(name.encode()) == ctypes.sizeof(cls)
 
 
@@ -67,3 +68,36 @@ def test_argument_errors_without_gpu(lib):
     assert b"null" in lib.mk_last_error()
     with pytest.raises(_lib.MKError):
         _lib.call("mk_camera_init", None, None, None)
+
+
+def test_tuning_switches_validate_without_gpu(lib):
+    """The measurement switches accept their documented values and refuse
+    others (no GPU call is made)."""
+    from mahakala_gb300 import _lib
+    for name, good, bad in ((b"fp64_rays_per_warp", (1, 32), (3, 64)), (b"fp64_zone", (0, 1), (2,)),
+                            (b"phase_events", (1, 0), (5,)), (b"f32_blocks_per_sm", (0, 3, 4, 5), (2, 6))):
+        for v in good:
+            _lib.call("mk_set_tuning", name, v)
+        for v in bad:
+            with pytest.raises(_lib.MKError) as e:
+                _lib.call("mk_set_tuning", name, v)
+            assert e.value.code == _lib.MK_ERR_ARG
+    _lib.call("mk_set_tuning", b"fp64_rays_per_warp", 32)
+    _lib.call("mk_set_tuning", b"fp64_zone", 1)
+    _lib.call("mk_set_tuning", b"phase_events", 0)
+    _lib.call("mk_set_tuning", b"f32_blocks_per_sm", 0)
+    with pytest.raises(_lib.MKError):
+        _lib.call("mk_set_tuning", b"no_such_knob", 1)
+
+
+def test_mixed_request_limit_without_gpu(lib):
+    """A mixed-form launch refuses more requests than its shared-memory
+    request table holds, before touching the device."""
+    import ctypes as c
+    from mahakala_gb300 import _lib
+    n = _lib.MK_MAX_REQUESTS_MIXED + 1
+    ws = (c.c_uint8 * 16)()
+    with pytest.raises(_lib.MKError) as e:
+        _lib.call("mk_render", c.addressof(ws), n, 10, c.addressof(ws), 1, _lib.MK_MIXED, c.addressof(ws),
+                  lib.mk_render_workspace_bytes(10, _lib.MK_MIXED), None)
+    assert e.value.code == _lib.MK_ERR_LIMIT

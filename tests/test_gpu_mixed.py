@@ -94,3 +94,47 @@ def test_sweep_corners_within_bar(cuda, medium_model):
     for r in rep["rows"]:
         assert r["max_step_optical_depth"] < 2.0, r
         assert r["flux_rel_err"] <= FLUX_TOL and r["max_pixel_rel_err"] <= PIX_TOL, r
+
+
+def test_phase_events_and_zone_switch(cuda, medium_model):
+    """Per-kernel CUDA events: one kernel for FP64, two for mixed, three for
+    mixed_strict, summing to the whole render; with the near-hole phase
+    switched off no ray leaves the FP32 phase and the image stays within
+    the bar."""
+    import ctypes
+
+    import torch
+
+    from mahakala_gb300 import _lib, metrics
+    from mahakala_gb300.images import PreparedRender, RenderRequest
+    kw = dict(camera_inclination=17.0, resolution=32, fov=50.0, max_nsteps=8192)
+    counts = {}
+    _lib.call("mk_set_tuning", b"phase_events", 1)
+    try:
+        for form, n in (("fp64", 1), ("mixed", 2), ("mixed_strict", 3)):
+            prep = PreparedRender([RenderRequest(medium_model, **kw)], precision=form)
+            prep.launch()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            prep.launch()
+            e1.record()
+            ms, got = (ctypes.c_float * 3)(), ctypes.c_int32()
+            _lib.call("mk_render_phase_ms", ms, ctypes.byref(got))
+            counts[form] = got.value
+            total = e0.elapsed_time(e1)
+            assert got.value == n
+            assert 0.5 * total <= sum(ms[:n]) <= 1.05 * total + 0.05
+    finally:
+        _lib.call("mk_set_tuning", b"phase_events", 0)
+    ref = PreparedRender([RenderRequest(medium_model, **kw)], precision="fp64")
+    ref.launch()
+    _lib.call("mk_set_tuning", b"fp64_zone", 0)
+    try:
+        prep = PreparedRender([RenderRequest(medium_model, **kw)], precision="mixed")
+        prep.launch()
+        assert prep.precision_split()[0] == 0
+    finally:
+        _lib.call("mk_set_tuning", b"fp64_zone", 1)
+    a, b = prep.images[0][0].cpu().numpy(), ref.images[0][0].cpu().numpy()
+    assert metrics.flux_rel_err(a, b) <= FLUX_TOL
+    assert metrics.max_pixel_rel_err(a, b) <= PIX_TOL
