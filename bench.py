@@ -560,7 +560,8 @@ def main():
                                   rays_per_side=srays)
 
     serving = None
-    if args.serving and not args.quick and args.workload == "render256":
+    if args.serving and not args.quick and args.workload == "render256" and rank == 0:
+        # one GPU's serving stream (the other replicas would repeat it)
         serving = run_serving(torch, model, args.serving, [f for f in ("mixed", "fp64") if f in forms])
 
     # end to end through the public API: host request in, NumPy image out
