@@ -577,6 +577,10 @@ def main():
         if k >= max(args.warmup, 3):
             e2e_times.append(time.perf_counter() - t0)
     e2e_t = statistics.mean(e2e_times) if e2e_times else float("nan")
+    if world > 1 and e2e_times:  # the slowest replica sets the job's rate
+        t = torch.tensor([e2e_t], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(t.item())
     L_unit = model.get_units(spec.M_bh, spec.mass_scale)["L_unit"]
 
     def roofline(form):

@@ -21,6 +21,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "mahakala_gb300.h"
 #include "mk_dd.cuh"
 
@@ -119,10 +121,6 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
 
     const T f = T(2.0f) * rr * r * iden;
     const T c1 = T(3.0f) * ir - T(4.0f) * rr * r * iden;
-    const T fx = f * (c1 * rx);
-    const T fy = f * (c1 * ry);
-    const T fz = f * (c1 * rz - T(2.0f) * aa * z * iden);
-
     const T l1 = (r * x + a * y) * ira;
     const T l2 = (r * y - a * x) * ira;
     const T l3 = z * ir;
@@ -130,20 +128,48 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
     const T g1 = (x - tr * l1) * ira;
     const T g2 = (y - tr * l2) * ira;
     const T rira = r * ira, aira = a * ira;
-    const T l1x = g1 * rx + rira, l1y = g1 * ry + aira, l1z = g1 * rz;
-    const T l2x = g2 * rx - aira, l2y = g2 * ry + rira, l2z = g2 * rz;
     const T h = z * ir * ir;
-    const T l3x = -h * rx, l3y = -h * ry, l3z = ir - h * rz;
 
+    // f and l_i depend on position through r and through the explicit x, y,
+    // z terms: grad l1 = g1 grad r + ira (r, a, 0), grad l2 = g2 grad r +
+    // ira (-a, r, 0), grad l3 = -h grad r + (0, 0, 1/r).  Below, D = k . grad
+    // and d = sum_i k_i grad l_i.
+    T Df, Dl1, Dl2, Dl3, dlx, dly, dlz, fx, fy, fz;
+    if constexpr (std::is_same<T, float>::value) {
+        // FP32: contract along k through k . grad r once (fewer operations
+        // than the nine gradient components; same value to rounding).
+        const T Dr = k1 * rx + k2 * ry + k3 * rz;
+        const T fc = f * c1;
+        const T ft = f * (T(2.0f) * aa * z * iden);
+        fx = fc * rx;
+        fy = fc * ry;
+        fz = fc * rz - ft;
+        Df = fc * Dr - ft * k3;
+        const T u1 = rira * k1, u2 = rira * k2, v1 = aira * k1, v2 = aira * k2;
+        Dl1 = g1 * Dr + (u1 + v2);
+        Dl2 = g2 * Dr + (u2 - v1);
+        Dl3 = ir * k3 - h * Dr;
+        const T G = g1 * k1 + g2 * k2 - h * k3;
+        dlx = rx * G + (u1 - v2);
+        dly = ry * G + (v1 + u2);
+        dlz = rz * G + ir * k3;
+    } else {
+        fx = f * (c1 * rx);
+        fy = f * (c1 * ry);
+        fz = f * (c1 * rz - T(2.0f) * aa * z * iden);
+        const T l1x = g1 * rx + rira, l1y = g1 * ry + aira, l1z = g1 * rz;
+        const T l2x = g2 * rx - aira, l2y = g2 * ry + rira, l2z = g2 * rz;
+        const T l3x = -h * rx, l3y = -h * ry, l3z = ir - h * rz;
+        Df = k1 * fx + k2 * fy + k3 * fz;
+        Dl1 = k1 * l1x + k2 * l1y + k3 * l1z;
+        Dl2 = k1 * l2x + k2 * l2y + k3 * l2z;
+        Dl3 = k1 * l3x + k2 * l3y + k3 * l3z;
+        dlx = l1x * k1 + l2x * k2 + l3x * k3;
+        dly = l1y * k1 + l2y * k2 + l3y * k3;
+        dlz = l1z * k1 + l2z * k2 + l3z * k3;
+    }
     const T lv = k0 + l1 * k1 + l2 * k2 + l3 * k3;
-    const T Df = k1 * fx + k2 * fy + k3 * fz;
-    const T Dl1 = k1 * l1x + k2 * l1y + k3 * l1z;
-    const T Dl2 = k1 * l2x + k2 * l2y + k3 * l2z;
-    const T Dl3 = k1 * l3x + k2 * l3y + k3 * l3z;
     const T Dlv = Dl1 * k1 + Dl2 * k2 + Dl3 * k3;
-    const T dlx = l1x * k1 + l2x * k2 + l3x * k3;
-    const T dly = l1y * k1 + l2y * k2 + l3y * k3;
-    const T dlz = l1z * k1 + l2z * k2 + l3z * k3;
 
     const T Dflv = Df * lv;
     const T fDlv = f * Dlv;
