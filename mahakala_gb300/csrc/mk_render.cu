@@ -24,10 +24,10 @@
 //     A  FP32 from the camera.  A ray whose radius drops below R_FP64 (3 M),
 //        or that moves inward inside R_TURN (6 M, where photon-ring rays
 //        reach their turning points), is handed to a queue (FP64 record);
-//     B  that queue (render_zone_kernel): near the hole the state is
-//        binary64, renormalised to null in binary64 on entry and at each
-//        radial turning point; a ray leaving R_TURN outward is renormalised
-//        once more and continues to its end on a float-pair state.
+//     B  that queue (render_zone_kernel): the float-pair state is
+//        renormalised to null in binary64 on entry, at each radial turning
+//        point and when the ray leaves R_TURN outward; the kernel carries the
+//        ray on to its end.
 //   MK_MIXED_STRICT: phase B integrates the near-hole geodesic entirely in
 //   binary64 (render_fp64_kernel over the queue) and parks rays leaving it
 //   for a third launch (phase C, FP32); MK_MIXED_DF: the same in
@@ -555,16 +555,16 @@ __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix,
     finish_ray(R, pix, Iout, steps, why, nsamples, (double)max_tau, ws);
 }
 
-// Mixed-form phase B (MK_MIXED): the rays near the hole.  The state is
-// held in binary64 and advanced by RK4 increments formed in float from the
-// state rounded to float (rk4_increment_f32); the wavevector is
-// renormalised to null in binary64 on entry and at every radial turning
-// point; the intensity and transmission sums are compensated floats.  The
-// accelerations and the emission are float, as in phases A and C: on this
-// part a binary64 acceleration costs ~33x a float one per step, and over
-// the measured images it changed the error against the FP64 form by less
-// than the float emission already contributes.  A ray leaving R_TURN
-// outward goes to the FP32 queue.
+// Mixed-form phase B (MK_MIXED): the rays near the hole.  The state is a
+// float pair per component (~48-bit significand), advanced by RK4
+// increments formed in float (rk4_increment_f32); the wavevector is
+// renormalised to null in binary64 on entry, at every radial turning point
+// and on leaving R_TURN outward; the intensity and transmission sums are
+// compensated floats.  The accelerations and the emission are float, as in
+// phase A: on this part a binary64 acceleration costs ~33x a float one per
+// step, and over the measured images it changed the error against the FP64
+// form by less than the float emission already contributes.  A ray leaving
+// R_TURN outward is counted as back in FP32 and continues here.
 //
 // Few rays reach this phase and its time is the serial chain of the
 // longest one, so each block runs two warps on two sub-partitions: warp 0
@@ -590,6 +590,15 @@ struct ZoneMsgs {
     float cdel[2][3][32];
 };
 
+// renull_fp64 on a float-pair state: only k^t changes
+__device__ __forceinline__ void renull_pair(const f2 X[4], f2 K[4], double a) {
+    double s[8];
+#pragma unroll
+    for (int i = 0; i < 4; i++) { s[i] = f2_to(X[i]); s[4 + i] = f2_to(K[i]); }
+    renull_fp64(s, a);
+    K[0] = f2_from(s[4]);
+}
+
 __device__ __forceinline__ void zone_barrier() {
     __syncwarp();  // the warp arrives converged
     asm volatile("bar.sync 1, 64;" ::: "memory");
@@ -604,12 +613,13 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
     bool active = false, exhausted = false;
     int rq = 0, steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0, b_steps = 0;
     long long ray = 0;
-    // near the hole: binary64 state s; after the ray leaves it outward the
-    // integration continues here on a float-pair state (X, K) as in the
-    // FP32 phases (the ray's remaining ~250 steps would otherwise wait for a
-    // third launch)
+    // float-pair state (X, K) throughout, as in the FP32 phases; near the
+    // hole the wavevector is renormalised to null in binary64 on entry, at
+    // every radial turning point and on the way out.  After the ray leaves
+    // outward the integration continues here to the ray's end (its
+    // remaining ~250 steps would otherwise wait for a third launch).
     bool inzone = true;
-    double s[8], bhspin = 0.0;
+    double bhspin = 0.0;
     f2 X[4], K[4];
     mk_snapshot_view sv;  // this ray's snapshot, loaded once
     float xf[8];  // the state rounded to float
@@ -623,6 +633,7 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
         if (idx == -1) exhausted = true;
         if (idx >= 0) {
             const RayRecord &q = q64[idx];
+            double s[8];
 #pragma unroll
             for (int i = 0; i < 8; i++) s[i] = q.s[i];
             ray = q.ray;
@@ -639,7 +650,12 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             sv = snaps[R.snapshot];
             sf = snap_f32(sv);
 #pragma unroll
-            for (int i = 0; i < 8; i++) xf[i] = (float)s[i];
+            for (int i = 0; i < 4; i++) {
+                X[i] = f2_from(s[i]);
+                K[i] = f2_from(s[4 + i]);
+                xf[i] = X[i].hi;
+                xf[4 + i] = K[i].hi;
+            }
             KerrPoint<float> m;
             kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3], m);
             r_cur = m.r;
@@ -662,35 +678,17 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
         if (active) {
             float xa[4], dK[4];
             rk4_increment_f32(xf, xf + 4, d1, dt, a, xa, dK);
-            double sn[8];
+            // pair-precision state update (a binary64 state cost the
+            // integrating warp 16 FP64-pipe instructions per step, ~1 k
+            // cycles of its chain, for no accuracy the float increments keep)
             f2 Xn[4], Kn[4];
             float xn[8];
-            if (inzone) {
-                // binary64 state; its float copy follows the float increments
-                // and is re-rounded from it every 8th step (a few float ulps of
-                // drift at most, below the float accelerations' own error; a
-                // binary64 -> float conversion per component and step held the
-                // integrating warp's issue for ~450 cycles)
-                float inc[8];
 #pragma unroll
-                for (int i = 0; i < 4; i++) { inc[i] = dt * xf[4 + i] + xa[i]; inc[4 + i] = dK[i]; }
-#pragma unroll
-                for (int i = 0; i < 8; i++) sn[i] = s[i] + (double)inc[i];
-                if ((run & 7) == 7) {
-#pragma unroll
-                    for (int i = 0; i < 8; i++) xn[i] = (float)sn[i];
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 8; i++) xn[i] = xf[i] + inc[i];
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    Xn[i] = f2_add(X[i], f2_add(f2_mul(K[i], dt), xa[i]));
-                    Kn[i] = f2_add(K[i], dK[i]);
-                    xn[i] = Xn[i].hi;
-                    xn[4 + i] = Kn[i].hi;
-                }
+            for (int i = 0; i < 4; i++) {
+                Xn[i] = f2_add(X[i], f2_add(f2_mul(K[i], dt), xa[i]));
+                Kn[i] = f2_add(K[i], dK[i]);
+                xn[i] = Xn[i].hi;
+                xn[4 + i] = Kn[i].hi;
             }
             CellPosF cell;
             const bool inside = locate_f32(sv, sf, xn[1], xn[2], xn[3], cell);
@@ -708,13 +706,8 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                 msg.steps[b][lane] = steps;
                 active = false;
             } else {
-                if (inzone) {
 #pragma unroll
-                    for (int i = 0; i < 8; i++) s[i] = sn[i];
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 4; i++) { X[i] = Xn[i]; K[i] = Kn[i]; }
-                }
+                for (int i = 0; i < 4; i++) { X[i] = Xn[i]; K[i] = Kn[i]; }
 #pragma unroll
                 for (int i = 0; i < 8; i++) xf[i] = xn[i];
 #pragma unroll
@@ -745,26 +738,18 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                     msg.why[b][lane] = MK_RAY_MAXSTEPS;
                     msg.steps[b][lane] = steps;
                     active = false;
-                } else if (inzone && r_new >= (float)R_TURN && dr > 0.0f) {
-                    // outbound past the photon-ring region: renormalise to null in
-                    // binary64 and continue on a float-pair state
-                    renull_fp64(s, bhspin);
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        X[i] = f2_from(s[i]);
-                        K[i] = f2_from(s[4 + i]);
-                        xf[i] = X[i].hi;
-                        xf[4 + i] = K[i].hi;
+                } else if (inzone && ((r_new >= (float)R_TURN && dr > 0.0f) ||
+                                      (dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f))) {
+                    // outbound past the photon-ring region, or a radial turning
+                    // point: renormalise to null in binary64 and re-evaluate the
+                    // first stage of the next step there
+                    renull_pair(X, K, bhspin);
+                    xf[4] = K[0].hi;
+                    kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3]);
+                    if (r_new >= (float)R_TURN && dr > 0.0f) {
+                        inzone = false;
+                        atomicAdd(&ws->q32_count, 1ull);  // counted as a ray back in FP32
                     }
-                    kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3]);
-                    inzone = false;
-                    atomicAdd(&ws->q32_count, 1ull);  // counted as a ray back in FP32
-                } else if (inzone && ((dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f))) {
-                    // radial turning point: renormalise to null in binary64 and
-                    // re-evaluate the first stage of the next step there
-                    renull_fp64(s, bhspin);
-                    xf[4] = (float)s[4];
-                    kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3]);
                 }
                 r_cur = r_new;
                 dr_prev = dr;
