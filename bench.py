@@ -546,8 +546,9 @@ def main():
         split = prep.precision_split() if form.startswith("mixed") else (0, 0, steps_total)
         samples64 = prep.samples_fp64() if form.startswith("mixed") else samples_total
         work_b = prep.phase_b_work() if form == "mixed" else None
+        work_c = prep.phase_c_work() if form.startswith("mixed") else None
         res[form] = dict(prep=prep, req=req, t_step=t_step, t_phase=t_phase, steps=steps_total,
-                         zone_run_max=prep.zone_run_max() if form == "mixed" else None, work_b=work_b,
+                         zone_run_max=prep.zone_run_max() if form == "mixed" else None, work_b=work_b, work_c=work_c,
                          samples=samples_total, samples64=samples64,
                          split=split, image=prep.images[0].clone(), status=req.out["status"].clone(),
                          max_tau=prep.max_step_optical_depth())
@@ -596,17 +597,18 @@ def main():
         else:
             to64, back32, steps64 = r["split"]
             stb, smb = r["work_b"] if r["work_b"] else (steps64, r["samples64"])
-            f32 = (r["steps"] - stb) * FLOP_PER_STEP + (r["samples"] - smb) * per_sample
-            # phase A does the FP32 steps up to the hand-off, phase C the rest;
-            # their split is not counted, so both carry the FP32 total over their sum
-            tA, tB, tC = (list(r["t_phase"]) + [0.0])[:3]   # MK_MIXED has no phase C
+            stc, smc = r["work_c"]
+            tA, tB, tC = r["t_phase"][:3]
+            fa = (r["steps"] - stb - stc) * FLOP_PER_STEP + (r["samples"] - smb - smc) * per_sample
             zone = stb * FLOP_PER_STEP + smb * per_sample
-            if form == "mixed":  # float accelerations and emission, binary64 state and sums
-                kb = ("render_zone_kernel (phase B: near the hole and after)", "fp32", zone, tB, peak32)
+            fc = stc * FLOP_PER_STEP + smc * per_sample
+            if form == "mixed":  # float accelerations and emission, float-pair state, compensated sums
+                kb = ("render_zone_kernel (phase B: near the hole and after; beside C)", "fp32", zone, tB, peak32)
+                kc = ("render_f32_kernel (phase C: parked outbound rays; beside B)", "fp32", fc, tC, peak32)
             else:
                 kb = ("render_fp64_kernel (phase B, near the hole)", "fp64", zone, tB, peak64)
-            ka = "render_f32_kernel (phase A)" if form == "mixed" else "render_f32_kernel (phases A+C)"
-            kernels = [(ka, "fp32", f32, tA + tC, peak32), kb]
+                kc = ("render_f32_kernel (phase C)", "fp32", fc, tC, peak32)
+            kernels = [("render_f32_kernel (phase A)", "fp32", fa, tA, peak32), kb, kc]
         table = [{"kernel": k, "bound": b, "flop": fl, "ms": 1e3 * t, "achieved": fl / t / 1e12 if t else None,
                   "peak": pk / 1e12, "frac": fl / t / pk if t else None} for k, b, fl, t, pk in kernels]
         top = max(table, key=lambda e: e["ms"])
@@ -681,7 +683,7 @@ def main():
                 "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
         "serving": serving,
         "sampling_stage": sampling,
-        "gpu_launches": args.steps * {"fp64": 1, "mixed": 2}.get(head, 3),
+        "gpu_launches": args.steps * {"fp64": 1}.get(head, 3),
         "phase_ms": {f: [1e3 * t for t in res[f]["t_phase"]] for f in forms},
         "clocks": clocks,
         "snapshot_build_s": t_gen,

@@ -270,16 +270,22 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
    in-snapshot samples, MK_WS_MAX_TAU the bits of a double, the largest
    per-step optical depth w*alpha of the transfer solve (the reference's
    explicit Euler update is stable below 1), MK_WS_TO_FP64 rays handed to
-   FP64, MK_WS_STEPS_FP64 steps and MK_WS_SAMPLES_FP64 in-snapshot samples
-   taken in FP64 (mixed form), MK_WS_ZONE_RUN_MAX the most steps one ray
-   took in one visit to the near-hole phase (MK_MIXED; its serial chain),
-   MK_WS_STEPS_B / MK_WS_SAMPLES_B the steps and samples MK_MIXED's second
-   launch took (near the hole and after). */
+   the near-hole phase, MK_WS_TO_FP32 rays that left it outward,
+   MK_WS_FP32_QUEUE rays in the FP32 continuation queue (MK_MIXED: rays
+   parked leaving the photon-ring region outward; the other mixed forms:
+   the near-hole phase's exits), MK_WS_STEPS_FP64 steps and
+   MK_WS_SAMPLES_FP64 in-snapshot samples taken near the hole (mixed
+   forms), MK_WS_ZONE_RUN_MAX the most steps one ray took in one visit to
+   the near-hole phase (MK_MIXED; its serial chain), MK_WS_STEPS_B /
+   MK_WS_SAMPLES_B the steps and samples MK_MIXED's near-hole kernel took
+   (near the hole and after), MK_WS_STEPS_C / MK_WS_SAMPLES_C those the
+   FP32 continuation kernel took (mixed forms). */
 #define MK_WS_STEPS 1
 #define MK_WS_SAMPLES 2
 #define MK_WS_MAX_TAU 3
 #define MK_WS_TO_FP64 4
-#define MK_WS_TO_FP32 6
+#define MK_WS_FP32_QUEUE 6
+#define MK_WS_TO_FP32 14
 #define MK_WS_STEPS_FP64 8
 #define MK_WS_SAMPLES_FP64 10
 #define MK_WS_ZONE_RUN_MAX 11
@@ -289,10 +295,15 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
 #define MK_MAX_REQUESTS_MIXED 128
 #define MK_WS_STEPS_B 12
 #define MK_WS_SAMPLES_B 13
+#define MK_WS_STEPS_C 15
+#define MK_WS_SAMPLES_C 16
 size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision);
 
 /* make_image (images.py:30-144) for nreq requests in ONE persistent launch
-   (three launches in the mixed form: FP32, FP64 near the hole, FP32):
+   (three in the mixed forms: FP32 from the camera, then the near-hole
+   phase and the FP32 continuation -- MK_MIXED runs these two at the same
+   time, the second on a per-thread side stream forked from and joined back
+   to `stream` with events, so a graph capture of `stream` takes both):
    camera -> geodesics -> sampling -> electrons -> synchrotron -> sigma cut ->
    transfer, fused per ray; no trajectory is stored.  reqs_dev (nreq)
    device array with ray_offset the exclusive prefix sum of the requests'
@@ -352,9 +363,9 @@ int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_ra
 int mk_set_tuning(const char *name, int64_t value);
 
 /* Durations (ms) of the kernels of the last render launched with the
-   "phase_events" tuning set, on the current device: one for MK_FP64, two
-   (phases A, B) for MK_MIXED, three (A, B, C) for MK_MIXED_STRICT and
-   MK_MIXED_DF; *nphases receives the count.
+   "phase_events" tuning set, on the current device: one for MK_FP64,
+   three (A, B, C) for the mixed forms -- in MK_MIXED, B and C both start
+   when A ends and run at the same time; *nphases receives the count.
    Waits for that render to finish.  No reference counterpart. */
 int mk_render_phase_ms(float *ms_out, int32_t *nphases);
 

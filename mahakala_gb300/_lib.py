@@ -26,10 +26,12 @@ MK_CAMERA_GRID, MK_CAMERA_EQUATOR = 0, 1
 MK_MAX_NU = 4
 NOALLOC_WORKSPACE_BYTES = 16 << 20
 NOALLOC_MAX_MIXED_RAYS = (NOALLOC_WORKSPACE_BYTES - 256) // 320
-MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_TO_FP32, MK_WS_STEPS_FP64 = 1, 2, 3, 4, 6, 8
+MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_FP32_QUEUE, MK_WS_STEPS_FP64 = 1, 2, 3, 4, 6, 8
+MK_WS_TO_FP32 = 14
 MK_WS_SAMPLES_FP64 = 10
 MK_WS_ZONE_RUN_MAX = 11
 MK_WS_STEPS_B, MK_WS_SAMPLES_B = 12, 13
+MK_WS_STEPS_C, MK_WS_SAMPLES_C = 15, 16
 MK_MAX_REQUESTS_MIXED = 128
 
 

@@ -47,6 +47,7 @@ namespace mk {
 constexpr int RENDER_THREADS = 128;
 constexpr double R_FP64 = 3.0;
 constexpr double R_TURN = 6.0;
+enum : int { F32_HANDOFF = 1, F32_PARK = 2 };
 
 // rays per warp in the mixed form's FP64 phase (mk_set_tuning
 // "fp64_rays_per_warp"): 32 fills every lane; fewer rays per warp shorten
@@ -69,8 +70,10 @@ static int g_phase_events = 0;
 static cudaEvent_t g_phase_ev[64][4];
 static bool g_phase_ev_made[64] = {false};
 static int g_phase_dev = -1, g_phase_n = 0;
+static int g_phase_from[4] = {0, 1, 2, 3};  // phase i runs from event g_phase_from[i] to event i + 1
 
-static int phase_mark(cudaStream_t st, int i) {
+// event i ends phase i - 1, which started at event `from`
+static int phase_mark(cudaStream_t st, int i, int from = -1) {
     if (!g_phase_events) return MK_OK;
     int dev = 0;
     MK_CUDA(cudaGetDevice(&dev));
@@ -82,6 +85,32 @@ static int phase_mark(cudaStream_t st, int i) {
     MK_CUDA(cudaEventRecord(g_phase_ev[dev][i], st));
     g_phase_dev = dev;
     g_phase_n = i;
+    if (i > 0) g_phase_from[i - 1] = from < 0 ? i - 1 : from;
+    return MK_OK;
+}
+
+// A second stream per host thread and device, with the two events that fork
+// it from and join it back to the caller's stream within one render.  Reused
+// across calls: a wait takes the event's latest record at the time it is
+// enqueued.  Created on a thread's first mixed-form render (an eager call;
+// a render captured into a graph records its fork and join as graph edges).
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+static int side_stream(SideStream **out) {
+    static thread_local SideStream t_side[64];
+    int dev = 0;
+    MK_CUDA(cudaGetDevice(&dev));
+    MK_REQUIRE(dev >= 0 && dev < 64, MK_ERR_LIMIT, "side stream: device ordinal %d not supported", dev);
+    SideStream &x = t_side[dev];
+    if (!x.s) {
+        MK_CUDA(cudaStreamCreateWithFlags(&x.s, cudaStreamNonBlocking));
+        MK_CUDA(cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming));
+        MK_CUDA(cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming));
+    }
+    *out = &x;
     return MK_OK;
 }
 
@@ -93,7 +122,7 @@ struct RenderWorkspace {
     unsigned long long max_tau_bits;  // max per-step optical depth w*alpha (bits of a double >= 0)
     unsigned long long q64_count;     // rays handed to FP64
     unsigned long long q64_next;
-    unsigned long long q32_count;     // rays handed back to FP32
+    unsigned long long q32_count;     // rays in the FP32 continuation queue
     unsigned long long q32_next;
     unsigned long long steps_fp64;    // accepted steps taken in FP64 (mixed form)
     unsigned long long overflow;      // queue overflow (cannot happen: capacity = rays)
@@ -101,6 +130,9 @@ struct RenderWorkspace {
     unsigned long long zone_run_max;  // most steps one ray took in one visit to the near-hole phase
     unsigned long long steps_b;       // all steps render_zone_kernel took (near the hole and after)
     unsigned long long samples_b;     // all samples render_zone_kernel took
+    unsigned long long zone_exits;    // rays that left the near-hole phase outward (back to FP32)
+    unsigned long long steps_c;       // steps the FP32 continuation over the FP32 queue took
+    unsigned long long samples_c;     // samples it took
 };
 constexpr size_t WS_HEADER = 256;
 static_assert(sizeof(RenderWorkspace) <= WS_HEADER, "workspace header");
@@ -522,6 +554,7 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
                 } else if (SRC == SRC_QUEUE && r_new >= R_TURN && r_new > r_cur) {
                     // outbound past the photon-ring region: back to FP32
                     const unsigned long long slot = atomicAdd(&ws->q32_count, 1ull);
+                    atomicAdd(&ws->zone_exits, 1ull);
                     if ((long long)slot < capacity) {
                         RayRecord &q = q32[slot];
 #pragma unroll
@@ -748,7 +781,7 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                     kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3]);
                     if (r_new >= (float)R_TURN && dr > 0.0f) {
                         inzone = false;
-                        atomicAdd(&ws->q32_count, 1ull);  // counted as a ray back in FP32
+                        atomicAdd(&ws->zone_exits, 1ull);
                     }
                 }
                 r_cur = r_new;
@@ -840,15 +873,17 @@ render_zone_kernel(const mk_request *__restrict__ reqs, const mk_snapshot_view *
 }
 
 
-// FP32 render phase.  SRC_CAMERA: mixed-form phase A from the camera, with
-// hand-off to the FP64 queue.  SRC_QUEUE: phase C over the FP32 queue.
+// FP32 render phase.  SRC_CAMERA: mixed-form phase A from the camera; mode
+// F32_HANDOFF hands rays near the hole to the near-hole queue, F32_PARK
+// parks rays leaving the photon-ring region outward in the FP32 queue.
+// SRC_QUEUE: the FP32 continuation over that queue (mode 0).
 // The ray state is a float pair per component (rk4_step_pair); the
 // accelerations, the sampling and the emission are plain float.
 template <int SRC, int MINB>
 __global__ void __launch_bounds__(RENDER_THREADS, MINB)
 render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
                   const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64, RayRecord *q32,
-                  long long capacity, const mk_job *job, int zone) {
+                  long long capacity, const mk_job *job, int mode) {
     if (job) {
         nreq = job->nreq;
         total_camera = job->total_rays;
@@ -867,6 +902,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
     f2 X[4], K[4];
     float d1[4], dt = 0.0f, r_cur = 0.0f, max_tau = 0.0f;
     float I[MK_MAX_NU], Ic[MK_MAX_NU], P[MK_MAX_NU];
+    int queue_steps = 0, queue_samples = 0;  // SRC_QUEUE: this thread's share of the launch's work
 
     for (;;) {
         const long long idx = fetch(!active && !exhausted, counter, total);
@@ -921,7 +957,13 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, active)) break;
+        if (!__any_sync(0xffffffffu, active)) {
+            if (SRC == SRC_QUEUE && queue_steps) {
+                atomicAdd(&ws->steps_c, (unsigned long long)queue_steps);
+                atomicAdd(&ws->samples_c, (unsigned long long)queue_samples);
+            }
+            break;
+        }
         if (active) {
             const mk_request &R = reqs[rq];
             // re-read the request constants every step: an address the
@@ -953,30 +995,41 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 ++steps;
                 const float sh[8] = {X[0].hi, X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi};
                 if (inside) sample_f32(sv, cell, Q.rc, sh, m, dt_used, I, Ic, P, Q.sc, nsamples, max_tau);
+                if (SRC == SRC_QUEUE) {
+                    ++queue_steps;
+                    queue_samples += inside;
+                }
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
                     active = false;
-                } else if (SRC == SRC_CAMERA && zone &&
-                           (r_new < (float)R_FP64 || (r_new < (float)R_TURN && r_new < r_cur))) {
-                    // near the horizon or inbound in the photon-ring region: FP64
-                    const unsigned long long slot = atomicAdd(&ws->q64_count, 1ull);
-                    if ((long long)slot < capacity) {
-                        RayRecord &q = q64[slot];
+                } else if (SRC == SRC_CAMERA && mode) {
+                    // near the horizon or inbound in the photon-ring region: to
+                    // the near-hole queue; outbound past it (F32_PARK): to the
+                    // FP32 continuation queue, whose kernel runs beside the
+                    // near-hole one
+                    const bool to64 = (mode & F32_HANDOFF) &&
+                                      (r_new < (float)R_FP64 || (r_new < (float)R_TURN && r_new < r_cur));
+                    const bool park = !to64 && (mode & F32_PARK) && r_new >= (float)R_TURN && r_new > r_cur;
+                    if (to64 || park) {
+                        const unsigned long long slot = atomicAdd(to64 ? &ws->q64_count : &ws->q32_count, 1ull);
+                        if ((long long)slot < capacity) {
+                            RayRecord &q = (to64 ? q64 : q32)[slot];
 #pragma unroll
-                        for (int i = 0; i < 4; i++) { q.s[i] = f2_to(X[i]); q.s[4 + i] = f2_to(K[i]); }
+                            for (int i = 0; i < 4; i++) { q.s[i] = f2_to(X[i]); q.s[4 + i] = f2_to(K[i]); }
 #pragma unroll
-                        for (int ch = 0; ch < MK_MAX_NU; ch++) {
-                            q.I[ch] = (double)I[ch] - (double)Ic[ch];
-                            q.P[ch] = (double)P[ch];
+                            for (int ch = 0; ch < MK_MAX_NU; ch++) {
+                                q.I[ch] = (double)I[ch] - (double)Ic[ch];
+                                q.P[ch] = (double)P[ch];
+                            }
+                            q.max_tau = (double)max_tau;
+                            q.ray = ray;
+                            q.steps = steps;
+                            q.nsamples = nsamples;
+                            q.rq = rq;
+                            active = false;
+                        } else {
+                            atomicAdd(&ws->overflow, 1ull);
                         }
-                        q.max_tau = (double)max_tau;
-                        q.ray = ray;
-                        q.steps = steps;
-                        q.nsamples = nsamples;
-                        q.rq = rq;
-                        active = false;
-                    } else {
-                        atomicAdd(&ws->overflow, 1ull);
                     }
                 }
                 r_cur = r_new;
@@ -1064,30 +1117,57 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     int f32_blocks = g_f32_blocks;
     if (f32_blocks == 0)
         f32_blocks = max_rays > (int64_t)device_sm_count() * 4 * RENDER_THREADS ? 5 : 4;
+    // MK_MIXED parks the outbound rays: its FP32 continuation then runs beside
+    // the near-hole phase instead of after it
+    const int mode = (g_fp64_zone ? F32_HANDOFF : 0) | (precision == MK_MIXED ? F32_PARK : 0);
     if (f32_blocks == 5)
         render_f32_kernel<SRC_CAMERA, 5>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 5>, 5), max_rays), RENDER_THREADS, 0,
-               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, g_fp64_zone);
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode);
     else if (f32_blocks == 4)
         render_f32_kernel<SRC_CAMERA, 4>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 4>, 1), max_rays), RENDER_THREADS, 0,
-               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, g_fp64_zone);
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode);
     else
         render_f32_kernel<SRC_CAMERA, 3>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 3>, 2), max_rays), RENDER_THREADS, 0,
-               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, g_fp64_zone);
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode);
     MK_LAUNCHED("render_f32_kernel (camera)");
     if ((rc = phase_mark(st, 1)) != MK_OK) return rc;
-    // The queues' sizes are only known on the device: persistent grids,
-    // small blocks, so the few rays near the hole spread over every SM
-    // sub-partition (they are latency-bound: one FP64 warp instruction holds
-    // a sub-partition's FP64 unit for tens of cycles on this part).
+    // The FP32 continuation over the FP32 queue; its size is only known on
+    // the device, so the grid is persistent.
+    auto launch_f32_queue = [&](cudaStream_t s) {
+        if (f32_blocks >= 4)
+            render_f32_kernel<SRC_QUEUE, 4>
+                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 4>, 3), max_rays), RENDER_THREADS, 0,
+                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
+        else
+            render_f32_kernel<SRC_QUEUE, 3>
+                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 3>, 4), max_rays), RENDER_THREADS, 0,
+                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
+    };
+    // The near-hole queue: persistent grids, small blocks, so the few rays
+    // near the hole spread over every SM sub-partition (they are
+    // latency-bound: one FP64 warp instruction holds a sub-partition's FP64
+    // unit for tens of cycles on this part).
     if (precision == MK_MIXED) {
-        // phase B carries its rays to their end: no phase C
+        // phase B (near the hole, then on to each ray's end) on the caller's
+        // stream and phase C (the parked outbound rays) on the side stream,
+        // at the same time: they share no ray and no counter
+        SideStream *side = nullptr;
+        if ((rc = side_stream(&side)) != MK_OK) return rc;
+        MK_CUDA(cudaEventRecord(side->fork, st));
+        MK_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
         render_zone_kernel<<<(unsigned)device_sm_count() * 4, ZONE_THREADS, 0, st>>>(reqs_dev, snaps_dev, ws, q64,
                                                                                       cap);
         MK_LAUNCHED("render_zone_kernel");
-        return phase_mark(st, 2);
+        launch_f32_queue(side->s);
+        MK_LAUNCHED("render_f32_kernel (queue)");
+        if ((rc = phase_mark(st, 2)) != MK_OK) return rc;
+        if ((rc = phase_mark(side->s, 3, 1)) != MK_OK) return rc;
+        MK_CUDA(cudaEventRecord(side->join, side->s));
+        MK_CUDA(cudaStreamWaitEvent(st, side->join, 0));
+        return MK_OK;
     }
     {
         const int per_warp = g_fp64_rays_per_warp;
@@ -1102,14 +1182,7 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
         MK_LAUNCHED("render_fp64_kernel (queue)");
     }
     if ((rc = phase_mark(st, 2)) != MK_OK) return rc;
-    if (f32_blocks >= 4)
-        render_f32_kernel<SRC_QUEUE, 4>
-            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 4>, 3), max_rays), RENDER_THREADS, 0,
-               st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
-    else
-        render_f32_kernel<SRC_QUEUE, 3>
-            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 3>, 4), max_rays), RENDER_THREADS, 0,
-               st>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
+    launch_f32_queue(st);
     MK_LAUNCHED("render_f32_kernel (queue)");
     return phase_mark(st, 3);
 }
@@ -1160,8 +1233,10 @@ extern "C" int mk_render_phase_ms(float *ms_out, int32_t *nphases) {
     MK_REQUIRE(cur == mk::g_phase_dev, MK_ERR_ARG, "mk_render_phase_ms: the last render ran on device %d",
                mk::g_phase_dev);
     cudaEvent_t *ev = mk::g_phase_ev[mk::g_phase_dev];
-    MK_CUDA(cudaEventSynchronize(ev[mk::g_phase_n]));
-    for (int i = 0; i < mk::g_phase_n; i++) MK_CUDA(cudaEventElapsedTime(&ms_out[i], ev[i], ev[i + 1]));
+    for (int i = 0; i < mk::g_phase_n; i++) {
+        MK_CUDA(cudaEventSynchronize(ev[i + 1]));
+        MK_CUDA(cudaEventElapsedTime(&ms_out[i], ev[mk::g_phase_from[i]], ev[i + 1]));
+    }
     *nphases = mk::g_phase_n;
     return MK_OK;
 }

@@ -165,6 +165,12 @@ class PreparedRender:
         w = self.ws[:32].cpu()
         return int(w[_lib.MK_WS_STEPS_B]), int(w[_lib.MK_WS_SAMPLES_B])
 
+    def phase_c_work(self):
+        """(steps, samples) the last mixed-form launch's FP32 continuation
+        kernel took (syncs)."""
+        w = self.ws[:32].cpu()
+        return int(w[_lib.MK_WS_STEPS_C]), int(w[_lib.MK_WS_SAMPLES_C])
+
     def zone_run_max(self):
         """Most steps one ray took in one visit to the mixed form's
         near-hole phase in the last launch (syncs): that phase's serial
