@@ -1137,7 +1137,11 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     // The FP32 continuation over the FP32 queue; its size is only known on
     // the device, so the grid is persistent.
     auto launch_f32_queue = [&](cudaStream_t s) {
-        if (f32_blocks >= 4)
+        if (f32_blocks == 5)
+            render_f32_kernel<SRC_QUEUE, 5>
+                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 5>, 6), max_rays), RENDER_THREADS, 0,
+                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
+        else if (f32_blocks == 4)
             render_f32_kernel<SRC_QUEUE, 4>
                 <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 4>, 3), max_rays), RENDER_THREADS, 0,
                    s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
