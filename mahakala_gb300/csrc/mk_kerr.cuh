@@ -92,104 +92,163 @@ __device__ __forceinline__ KerrPoint<T> kerr_point(T x, T y, T z, T a) {
     return m;
 }
 
+// The FP32 geodesic acceleration (mixed-precision phases).  Same
+// contraction as the generic form below, rearranged for fewer
+// instructions: f and l_i depend on position through r and through explicit
+// x, y, z terms -- grad l1 = g1 grad r + (r, a, 0)/(r^2 + a^2), grad l2 =
+// g2 grad r + (-a, r, 0)/(r^2 + a^2), grad l3 = -h grad r + (0, 0, 1/r) --
+// so the derivatives along k (D = k . grad) and the sums d = sum_i k_i
+// grad l_i come from k . grad r without the nine gradient components, and
+// F_i = l_i F_0 + f (k.l) (d_i - D l_i) + f_i (k.l)^2 / 2.  The x and y
+// components go through paired FP32 instructions (two lanes of one
+// instruction, each rounded as its scalar twin).  Equal to the generic form
+// to float rounding.
+__device__ __forceinline__ float2 pair(float u, float v) { return make_float2(u, v); }
+__device__ __forceinline__ float2 both(float u) { return make_float2(u, u); }
+
+__device__ __forceinline__ void kerr_accel_f32(float x, float y, float z, float k0, float k1, float k2, float k3,
+                                               float a, float &a0, float &a1, float &a2, float &a3,
+                                               KerrPoint<float> &m) {
+    const float2 XY = pair(x, y), K12 = pair(k1, k2);
+    const float aa = a * a;
+    const float zz = z * z;
+    const float kk = 0.5f * (x * x + y * y + zz - aa);
+    const float Q = kk * kk + aa * zz;
+    const float iq = inv_sqrt(Q);
+    const float q = Q * iq;                  // sqrt(kk^2 + a^2 z^2)
+    const float rr = q + kk;
+    const float ir = inv_sqrt(rr);
+    const float r = rr * ir;
+    const float i2rq = 0.5f * ir * iq;       // 1 / (2 r q)
+    const float den = rr * rr + aa * zz;
+    const float rra = rr + aa;
+    // one division for the two reciprocals 1/den and 1/(rr + a^2)
+    const float inv2 = fdiv(1.0f, den * rra);
+    const float2 ID = __fmul2_rn(pair(rra, den), both(inv2));
+    const float iden = ID.x, ira = ID.y;
+    const float2 RXY = __fmul2_rn(both(rr * i2rq), XY);  // (dr/dx, dr/dy)
+    const float rz = rra * z * i2rq;
+    const float rrr = rr * r;
+    const float f = 2.0f * rrr * iden;
+    const float c1 = 3.0f * ir - 4.0f * rrr * iden;
+    // (l1, l2) = (r x + a y, r y - a x) / (r^2 + a^2); (g1, g2) = (xy - 2 r l) / (r^2 + a^2)
+    const float2 L12 = __fmul2_rn(__ffma2_rn(both(r), XY, __fmul2_rn(both(a), pair(y, -x))), both(ira));
+    const float l3 = z * ir;
+    const float2 G12 = __fmul2_rn(__ffma2_rn(both(-2.0f * r), L12, XY), both(ira));
+    const float rira = r * ira, aira = a * ira;
+    const float h = z * ir * ir;
+    const float Dr = k1 * RXY.x + k2 * RXY.y + k3 * rz;
+    const float fc = f * c1;
+    const float ft = f * (2.0f * aa * z * iden);
+    const float2 FXY = __fmul2_rn(both(fc), RXY);
+    const float fz = fc * rz - ft;
+    const float Df = fc * Dr - ft * k3;
+    const float2 U = __fmul2_rn(both(rira), K12), V = __fmul2_rn(both(aira), K12);
+    const float2 DL12 = __ffma2_rn(G12, both(Dr), __fadd2_rn(U, pair(V.y, -V.x)));   // D l1, D l2
+    const float Dl3 = ir * k3 - h * Dr;
+    const float G = G12.x * k1 + G12.y * k2 - h * k3;
+    const float2 DLXY = __ffma2_rn(RXY, both(G), __fadd2_rn(pair(U.x, V.x), pair(-V.y, U.y)));  // d_x, d_y
+    const float dlz = rz * G + ir * k3;
+    const float lv = k0 + L12.x * k1 + L12.y * k2 + l3 * k3;
+    const float Dlv = DL12.x * k1 + DL12.y * k2 + Dl3 * k3;
+    const float flv = f * lv;
+    const float hl = 0.5f * lv * lv;
+    const float F0 = -(Df * lv + f * Dlv);
+    const float2 F12 =
+        __ffma2_rn(FXY, both(hl), __ffma2_rn(both(flv), __fadd2_rn(DLXY, pair(-DL12.x, -DL12.y)), __fmul2_rn(L12, both(F0))));
+    const float F3 = l3 * F0 + flv * (dlz - Dl3) + fz * hl;
+    const float lF = -F0 + L12.x * F12.x + L12.y * F12.y + l3 * F3;
+    const float flF = f * lF;
+    const float2 A12 = __ffma2_rn(L12, both(-flF), F12);
+    a0 = -F0 + flF;
+    a1 = A12.x;
+    a2 = A12.y;
+    a3 = F3 - l3 * flF;
+    m.r = r;
+    m.f = f;
+    m.l1 = L12.x;
+    m.l2 = L12.y;
+    m.l3 = l3;
+}
+
 // Geodesic acceleration dk/dlambda = -Gamma^mu_ab k^a k^b at (x, y, z).
 // Also returns the metric data at the point (r, f, l), which the step rule
 // and the sampler reuse.
 template <typename T>
 __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3, T a, T &a0, T &a1, T &a2,
                                            T &a3, KerrPoint<T> &m) {
-    const T aa = a * a;
-    const T zz = z * z;
-    const T kk = T(0.5f) * (x * x + y * y + zz - aa);
-    const T Q = kk * kk + aa * zz;
-    const T iq = inv_sqrt(Q);
-    const T q = Q * iq;                      // sqrt(kk^2 + a^2 z^2)
-    const T rr = q + kk;
-    const T ir = inv_sqrt(rr);
-    const T r = rr * ir;
-    const T i2rq = T(0.5f) * ir * iq;         // 1 / (2 r q)
-    const T den = rr * rr + aa * zz;
-    const T rra = rr + aa;
-    // one division for the two reciprocals 1/den and 1/(rr + a^2)
-    const T inv2 = fdiv(T(1.0f), den * rra);
-    const T iden = rra * inv2;
-    const T ira = den * inv2;
-
-    const T rx = rr * x * i2rq;
-    const T ry = rr * y * i2rq;
-    const T rz = rra * z * i2rq;
-
-    const T f = T(2.0f) * rr * r * iden;
-    const T c1 = T(3.0f) * ir - T(4.0f) * rr * r * iden;
-    const T l1 = (r * x + a * y) * ira;
-    const T l2 = (r * y - a * x) * ira;
-    const T l3 = z * ir;
-    const T tr = T(2.0f) * r;
-    const T g1 = (x - tr * l1) * ira;
-    const T g2 = (y - tr * l2) * ira;
-    const T rira = r * ira, aira = a * ira;
-    const T h = z * ir * ir;
-
-    // f and l_i depend on position through r and through the explicit x, y,
-    // z terms: grad l1 = g1 grad r + ira (r, a, 0), grad l2 = g2 grad r +
-    // ira (-a, r, 0), grad l3 = -h grad r + (0, 0, 1/r).  Below, D = k . grad
-    // and d = sum_i k_i grad l_i.
-    T Df, Dl1, Dl2, Dl3, dlx, dly, dlz, fx, fy, fz;
     if constexpr (std::is_same<T, float>::value) {
-        // FP32: contract along k through k . grad r once (fewer operations
-        // than the nine gradient components; same value to rounding).
-        const T Dr = k1 * rx + k2 * ry + k3 * rz;
-        const T fc = f * c1;
-        const T ft = f * (T(2.0f) * aa * z * iden);
-        fx = fc * rx;
-        fy = fc * ry;
-        fz = fc * rz - ft;
-        Df = fc * Dr - ft * k3;
-        const T u1 = rira * k1, u2 = rira * k2, v1 = aira * k1, v2 = aira * k2;
-        Dl1 = g1 * Dr + (u1 + v2);
-        Dl2 = g2 * Dr + (u2 - v1);
-        Dl3 = ir * k3 - h * Dr;
-        const T G = g1 * k1 + g2 * k2 - h * k3;
-        dlx = rx * G + (u1 - v2);
-        dly = ry * G + (v1 + u2);
-        dlz = rz * G + ir * k3;
+        kerr_accel_f32(x, y, z, k0, k1, k2, k3, a, a0, a1, a2, a3, m);
     } else {
-        fx = f * (c1 * rx);
-        fy = f * (c1 * ry);
-        fz = f * (c1 * rz - T(2.0f) * aa * z * iden);
+        const T aa = a * a;
+        const T zz = z * z;
+        const T kk = T(0.5f) * (x * x + y * y + zz - aa);
+        const T Q = kk * kk + aa * zz;
+        const T iq = inv_sqrt(Q);
+        const T q = Q * iq;                      // sqrt(kk^2 + a^2 z^2)
+        const T rr = q + kk;
+        const T ir = inv_sqrt(rr);
+        const T r = rr * ir;
+        const T i2rq = T(0.5f) * ir * iq;         // 1 / (2 r q)
+        const T den = rr * rr + aa * zz;
+        const T rra = rr + aa;
+        // one division for the two reciprocals 1/den and 1/(rr + a^2)
+        const T inv2 = fdiv(T(1.0f), den * rra);
+        const T iden = rra * inv2;
+        const T ira = den * inv2;
+
+        const T rx = rr * x * i2rq;
+        const T ry = rr * y * i2rq;
+        const T rz = rra * z * i2rq;
+
+        const T f = T(2.0f) * rr * r * iden;
+        const T c1 = T(3.0f) * ir - T(4.0f) * rr * r * iden;
+        const T fx = f * (c1 * rx);
+        const T fy = f * (c1 * ry);
+        const T fz = f * (c1 * rz - T(2.0f) * aa * z * iden);
+
+        const T l1 = (r * x + a * y) * ira;
+        const T l2 = (r * y - a * x) * ira;
+        const T l3 = z * ir;
+        const T tr = T(2.0f) * r;
+        const T g1 = (x - tr * l1) * ira;
+        const T g2 = (y - tr * l2) * ira;
+        const T rira = r * ira, aira = a * ira;
         const T l1x = g1 * rx + rira, l1y = g1 * ry + aira, l1z = g1 * rz;
         const T l2x = g2 * rx - aira, l2y = g2 * ry + rira, l2z = g2 * rz;
+        const T h = z * ir * ir;
         const T l3x = -h * rx, l3y = -h * ry, l3z = ir - h * rz;
-        Df = k1 * fx + k2 * fy + k3 * fz;
-        Dl1 = k1 * l1x + k2 * l1y + k3 * l1z;
-        Dl2 = k1 * l2x + k2 * l2y + k3 * l2z;
-        Dl3 = k1 * l3x + k2 * l3y + k3 * l3z;
-        dlx = l1x * k1 + l2x * k2 + l3x * k3;
-        dly = l1y * k1 + l2y * k2 + l3y * k3;
-        dlz = l1z * k1 + l2z * k2 + l3z * k3;
-    }
-    const T lv = k0 + l1 * k1 + l2 * k2 + l3 * k3;
-    const T Dlv = Dl1 * k1 + Dl2 * k2 + Dl3 * k3;
 
-    const T Dflv = Df * lv;
-    const T fDlv = f * Dlv;
-    const T half_lv2 = T(0.5f) * lv * lv;
-    const T flv = f * lv;
-    const T F0 = -(Dflv + fDlv);
-    const T F1 = -(Dflv * l1 + f * (Dl1 * lv) + l1 * fDlv) + fx * half_lv2 + flv * dlx;
-    const T F2 = -(Dflv * l2 + f * (Dl2 * lv) + l2 * fDlv) + fy * half_lv2 + flv * dly;
-    const T F3 = -(Dflv * l3 + f * (Dl3 * lv) + l3 * fDlv) + fz * half_lv2 + flv * dlz;
-    const T lF = -F0 + l1 * F1 + l2 * F2 + l3 * F3;
-    const T flF = f * lF;
-    a0 = -F0 + flF;
-    a1 = F1 - l1 * flF;
-    a2 = F2 - l2 * flF;
-    a3 = F3 - l3 * flF;
-    m.r = r;
-    m.f = f;
-    m.l1 = l1;
-    m.l2 = l2;
-    m.l3 = l3;
+        const T lv = k0 + l1 * k1 + l2 * k2 + l3 * k3;
+        const T Df = k1 * fx + k2 * fy + k3 * fz;
+        const T Dl1 = k1 * l1x + k2 * l1y + k3 * l1z;
+        const T Dl2 = k1 * l2x + k2 * l2y + k3 * l2z;
+        const T Dl3 = k1 * l3x + k2 * l3y + k3 * l3z;
+        const T Dlv = Dl1 * k1 + Dl2 * k2 + Dl3 * k3;
+        const T dlx = l1x * k1 + l2x * k2 + l3x * k3;
+        const T dly = l1y * k1 + l2y * k2 + l3y * k3;
+        const T dlz = l1z * k1 + l2z * k2 + l3z * k3;
+
+        const T Dflv = Df * lv;
+        const T fDlv = f * Dlv;
+        const T half_lv2 = T(0.5f) * lv * lv;
+        const T flv = f * lv;
+        const T F0 = -(Dflv + fDlv);
+        const T F1 = -(Dflv * l1 + f * (Dl1 * lv) + l1 * fDlv) + fx * half_lv2 + flv * dlx;
+        const T F2 = -(Dflv * l2 + f * (Dl2 * lv) + l2 * fDlv) + fy * half_lv2 + flv * dly;
+        const T F3 = -(Dflv * l3 + f * (Dl3 * lv) + l3 * fDlv) + fz * half_lv2 + flv * dlz;
+        const T lF = -F0 + l1 * F1 + l2 * F2 + l3 * F3;
+        const T flF = f * lF;
+        a0 = -F0 + flF;
+        a1 = F1 - l1 * flF;
+        a2 = F2 - l2 * flF;
+        a3 = F3 - l3 * flF;
+        m.r = r;
+        m.f = f;
+        m.l1 = l1;
+        m.l2 = l2;
+        m.l3 = l3;
+    }
 }
 
 template <typename T>
