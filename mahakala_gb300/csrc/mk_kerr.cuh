@@ -343,6 +343,68 @@ __device__ __forceinline__ f2 f2_from(double d) {
 
 __device__ __forceinline__ double f2_to(f2 x) { return (double)x.hi + (double)x.lo; }
 
+// The same operations on two components at once (float2 lanes), on paired
+// FP32 instructions; every lane rounds exactly as the scalar steps above
+// (x - y is formed as fma(y, -1, x), -p as the product with -b).
+struct f2v {
+    float2 hi, lo;
+};
+
+__device__ __forceinline__ f2v f2v_of(f2 u, f2 v) { return {pair(u.hi, v.hi), pair(u.lo, v.lo)}; }
+__device__ __forceinline__ f2 f2v_x(f2v p) { return {p.hi.x, p.lo.x}; }
+__device__ __forceinline__ f2 f2v_y(f2v p) { return {p.hi.y, p.lo.y}; }
+__device__ __forceinline__ float2 sub2(float2 x, float2 y) { return __ffma2_rn(y, both(-1.0f), x); }
+
+__device__ __forceinline__ f2v two_sum2(float2 a, float2 b) {
+    const float2 s = __fadd2_rn(a, b);
+    const float2 v = sub2(s, a);
+    return {s, __fadd2_rn(sub2(a, sub2(s, v)), sub2(b, v))};
+}
+
+__device__ __forceinline__ f2v fast_two_sum2(float2 a, float2 b) {
+    const float2 s = __fadd2_rn(a, b);
+    return {s, sub2(b, sub2(s, a))};
+}
+
+__device__ __forceinline__ f2v f2v_add(f2v x, float2 y) {
+    f2v s = two_sum2(x.hi, y);
+    s.lo = __fadd2_rn(s.lo, x.lo);
+    return fast_two_sum2(s.hi, s.lo);
+}
+
+__device__ __forceinline__ f2v f2v_add(f2v x, f2v y) {
+    f2v s = two_sum2(x.hi, y.hi);
+    s.lo = __fadd2_rn(s.lo, __fadd2_rn(x.lo, y.lo));
+    return fast_two_sum2(s.hi, s.lo);
+}
+
+__device__ __forceinline__ f2v f2v_mul(f2v x, float b) {
+    const float2 p = __fmul2_rn(x.hi, both(b));
+    float2 e = __ffma2_rn(x.hi, both(b), __fmul2_rn(x.hi, both(-b)));
+    e = __ffma2_rn(x.lo, both(b), e);
+    return fast_two_sum2(p, e);
+}
+
+// The float-pair state update of one RK4 step: X += dt K + dXa, K += dK,
+// components 1 and 2 and (of K) 0-1 and 2-3 in pairs.  The time coordinate
+// X[0] is not advanced: nothing on the imaging path reads it (the sampler
+// and the step rule use the metric at x^1..x^3 and k), so the float phases
+// leave it at its value from the camera.
+__device__ __forceinline__ void pair_state_update(const f2 X[4], const f2 K[4], float dt, const float dXa[4],
+                                                  const float dK[4], f2 Xo[4], f2 Ko[4]) {
+    const f2v x12 = f2v_add(f2v_of(X[1], X[2]), f2v_add(f2v_mul(f2v_of(K[1], K[2]), dt), pair(dXa[1], dXa[2])));
+    Xo[0] = X[0];
+    Xo[1] = f2v_x(x12);
+    Xo[2] = f2v_y(x12);
+    Xo[3] = f2_add(X[3], f2_add(f2_mul(K[3], dt), dXa[3]));
+    const f2v k01 = f2v_add(f2v_of(K[0], K[1]), pair(dK[0], dK[1]));
+    const f2v k23 = f2v_add(f2v_of(K[2], K[3]), pair(dK[2], dK[3]));
+    Ko[0] = f2v_x(k01);
+    Ko[1] = f2v_y(k01);
+    Ko[2] = f2v_x(k23);
+    Ko[3] = f2v_y(k23);
+}
+
 // RK4 on a float-pair state (X = x^mu, K = k^mu), accelerations in float.
 // The position increment of RK4 is dt k + dt^2/6 (a1 + a2 + a3); its
 // leading term is formed in pair precision, so neither rounding of the
@@ -365,11 +427,13 @@ __device__ __forceinline__ void rk4_step_pair(const f2 X[4], const f2 K[4], cons
     kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a4[0], a4[1], a4[2], a4[3]);
     const float c = dt * dt * (1.0f / 6.0f);
     const float d = dt * (1.0f / 6.0f);
+    float dXa[4], dK[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        Xo[i] = f2_add(X[i], f2_add(f2_mul(K[i], dt), c * (a1[i] + a2[i] + a3[i])));
-        Ko[i] = f2_add(K[i], d * (a1[i] + 2.0f * a2[i] + 2.0f * a3[i] + a4[i]));
+        dXa[i] = c * (a1[i] + a2[i] + a3[i]);
+        dK[i] = d * (a1[i] + 2.0f * a2[i] + 2.0f * a3[i] + a4[i]);
     }
+    pair_state_update(X, K, dt, dXa, dK, Xo, Ko);
 }
 
 // The RK4 increments of one step in float, for a state held elsewhere in

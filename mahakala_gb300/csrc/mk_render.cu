@@ -716,10 +716,9 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             // cycles of its chain, for no accuracy the float increments keep)
             f2 Xn[4], Kn[4];
             float xn[8];
+            pair_state_update(X, K, dt, xa, dK, Xn, Kn);
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                Xn[i] = f2_add(X[i], f2_add(f2_mul(K[i], dt), xa[i]));
-                Kn[i] = f2_add(K[i], dK[i]);
                 xn[i] = Xn[i].hi;
                 xn[4 + i] = Kn[i].hi;
             }
