@@ -392,7 +392,9 @@ __device__ __forceinline__ void trilinear8_f32(const mk_snapshot_view &s, const 
     const int n2 = s.n + 2;
     const int64_t sj = (int64_t)n2 * 8, sk = (int64_t)n2 * n2 * 8;
     const float *base = s.blocks + ((((int64_t)c.mb * n2 + c.idx[2]) * n2 + c.idx[1]) * n2 + c.idx[0]) * 8;
-    float v[2][2][2][8];
+    // primitives in pairs (0-1, 2-3, 4-5, 6-7), lerped on paired FP32
+    // instructions: each lane is fma(b - a, d, a) as in the scalar form
+    float2 v[2][2][2][4];
 #pragma unroll
     for (int dk = 0; dk < 2; dk++)
 #pragma unroll
@@ -401,19 +403,25 @@ __device__ __forceinline__ void trilinear8_f32(const mk_snapshot_view &s, const 
             for (int di = 0; di < 2; di++) {
                 const float *p = base + dk * sk + dj * sj + di * 8;
                 const float4 lo = ldg4(p), hi = ldg4(p + 4);
-                v[dk][dj][di][0] = lo.x; v[dk][dj][di][1] = lo.y; v[dk][dj][di][2] = lo.z; v[dk][dj][di][3] = lo.w;
-                v[dk][dj][di][4] = hi.x; v[dk][dj][di][5] = hi.y; v[dk][dj][di][6] = hi.z; v[dk][dj][di][7] = hi.w;
+                v[dk][dj][di][0] = make_float2(lo.x, lo.y);
+                v[dk][dj][di][1] = make_float2(lo.z, lo.w);
+                v[dk][dj][di][2] = make_float2(hi.x, hi.y);
+                v[dk][dj][di][3] = make_float2(hi.z, hi.w);
             }
-    const float d1 = c.del[0], d2 = c.del[1], d3 = c.del[2];
+    const float2 d1 = make_float2(c.del[0], c.del[0]), d2 = make_float2(c.del[1], c.del[1]),
+                 d3 = make_float2(c.del[2], c.del[2]), m1 = make_float2(-1.0f, -1.0f);
+    auto lerp = [&](float2 a, float2 b, float2 d) { return __ffma2_rn(__ffma2_rn(a, m1, b), d, a); };
 #pragma unroll
-    for (int p = 0; p < 8; p++) {
-        const float daa = fmaf(v[0][0][1][p] - v[0][0][0][p], d1, v[0][0][0][p]);
-        const float dab = fmaf(v[0][1][1][p] - v[0][1][0][p], d1, v[0][1][0][p]);
-        const float dba = fmaf(v[1][0][1][p] - v[1][0][0][p], d1, v[1][0][0][p]);
-        const float dbb = fmaf(v[1][1][1][p] - v[1][1][0][p], d1, v[1][1][0][p]);
-        const float da = fmaf(dab - daa, d2, daa);
-        const float db = fmaf(dbb - dba, d2, dba);
-        prim[p] = fmaf(db - da, d3, da);
+    for (int p = 0; p < 4; p++) {
+        const float2 daa = lerp(v[0][0][0][p], v[0][0][1][p], d1);
+        const float2 dab = lerp(v[0][1][0][p], v[0][1][1][p], d1);
+        const float2 dba = lerp(v[1][0][0][p], v[1][0][1][p], d1);
+        const float2 dbb = lerp(v[1][1][0][p], v[1][1][1][p], d1);
+        const float2 da = lerp(daa, dab, d2);
+        const float2 db = lerp(dba, dbb, d2);
+        const float2 r = lerp(da, db, d3);
+        prim[2 * p] = r.x;
+        prim[2 * p + 1] = r.y;
     }
 }
 

@@ -386,7 +386,7 @@ __device__ __forceinline__ f2v f2v_mul(f2v x, float b) {
 }
 
 // The float-pair state update of one RK4 step: X += dt K + dXa, K += dK,
-// components 1 and 2 and (of K) 0-1 and 2-3 in pairs.  The time coordinate
+// components 1-2 and (of K) 0-3 in pairs.  The time coordinate
 // X[0] is not advanced: nothing on the imaging path reads it (the sampler
 // and the step rule use the metric at x^1..x^3 and k), so the float phases
 // leave it at its value from the camera.
@@ -397,12 +397,57 @@ __device__ __forceinline__ void pair_state_update(const f2 X[4], const f2 K[4], 
     Xo[1] = f2v_x(x12);
     Xo[2] = f2v_y(x12);
     Xo[3] = f2_add(X[3], f2_add(f2_mul(K[3], dt), dXa[3]));
-    const f2v k01 = f2v_add(f2v_of(K[0], K[1]), pair(dK[0], dK[1]));
-    const f2v k23 = f2v_add(f2v_of(K[2], K[3]), pair(dK[2], dK[3]));
-    Ko[0] = f2v_x(k01);
-    Ko[1] = f2v_y(k01);
-    Ko[2] = f2v_x(k23);
-    Ko[3] = f2v_y(k23);
+    const f2v k12 = f2v_add(f2v_of(K[1], K[2]), pair(dK[1], dK[2]));
+    const f2v k03 = f2v_add(f2v_of(K[0], K[3]), pair(dK[0], dK[3]));
+    Ko[0] = f2v_x(k03);
+    Ko[1] = f2v_x(k12);
+    Ko[2] = f2v_y(k12);
+    Ko[3] = f2v_y(k03);
+}
+
+// The three inner stages and the combination of one RK4 step in float
+// (RK4_gen, geodesics.py:317-336, written for x'' = a(x, x')): x, k the
+// state in float, a1 the acceleration there.  Returns dXa = dt^2/6 (a1 + a2
+// + a3) (the position increment is dt k + dXa; the caller forms dt k in its
+// own precision) and dK = dt/6 (a1 + 2 a2 + 2 a3 + a4).  Components 1-2 and
+// 0-3 go in pairs through paired FP32 instructions, each lane formed as
+// the scalar fma(h, k, x) chain.
+__device__ __forceinline__ void rk4_stages_f32(const float x[4], const float k[4], const float a1[4], float dt,
+                                               float a, float dXa[4], float dK[4]) {
+    const float h = 0.5f * dt;
+    const float2 H = both(h), DT = both(dt);
+    const float2 x12 = pair(x[1], x[2]), k12 = pair(k[1], k[2]), k03 = pair(k[0], k[3]);
+    const float2 a1_12 = pair(a1[1], a1[2]), a1_03 = pair(a1[0], a1[3]);
+    float a2[4], a3[4], a4[4];
+    // stage 2 at (x + h k, k + h a1)
+    const float2 s12 = __ffma2_rn(H, a1_12, k12), s03 = __ffma2_rn(H, a1_03, k03);
+    float2 p12 = __ffma2_rn(H, k12, x12);
+    kerr_accel(p12.x, p12.y, fmaf(h, k[3], x[3]), s03.x, s12.x, s12.y, s03.y, a, a2[0], a2[1], a2[2], a2[3]);
+    // stage 3 at (x + h (k + h a1), k + h a2)
+    const float2 a2_12 = pair(a2[1], a2[2]), a2_03 = pair(a2[0], a2[3]);
+    const float2 u12 = __ffma2_rn(H, a2_12, k12), u03 = __ffma2_rn(H, a2_03, k03);
+    p12 = __ffma2_rn(H, s12, x12);
+    kerr_accel(p12.x, p12.y, fmaf(h, s03.y, x[3]), u03.x, u12.x, u12.y, u03.y, a, a3[0], a3[1], a3[2], a3[3]);
+    // stage 4 at (x + dt (k + h a2), k + dt a3)
+    const float2 a3_12 = pair(a3[1], a3[2]), a3_03 = pair(a3[0], a3[3]);
+    const float2 w12 = __ffma2_rn(DT, a3_12, k12), w03 = __ffma2_rn(DT, a3_03, k03);
+    p12 = __ffma2_rn(DT, u12, x12);
+    kerr_accel(p12.x, p12.y, fmaf(dt, u03.y, x[3]), w03.x, w12.x, w12.y, w03.y, a, a4[0], a4[1], a4[2], a4[3]);
+    const float c = dt * dt * (1.0f / 6.0f);
+    const float d = dt * (1.0f / 6.0f);
+    const float2 C = both(c), D = both(d), TWO = both(2.0f);
+    const float2 a4_12 = pair(a4[1], a4[2]), a4_03 = pair(a4[0], a4[3]);
+    const float2 x_12 = __fmul2_rn(C, __fadd2_rn(__fadd2_rn(a1_12, a2_12), a3_12));
+    const float2 k_12 = __fmul2_rn(D, __fadd2_rn(__ffma2_rn(TWO, a3_12, __ffma2_rn(TWO, a2_12, a1_12)), a4_12));
+    const float2 k_03 = __fmul2_rn(D, __fadd2_rn(__ffma2_rn(TWO, a3_03, __ffma2_rn(TWO, a2_03, a1_03)), a4_03));
+    dXa[0] = 0.0f;  // the time coordinate is not advanced (pair_state_update)
+    dXa[1] = x_12.x;
+    dXa[2] = x_12.y;
+    dXa[3] = c * (a1[3] + a2[3] + a3[3]);
+    dK[0] = k_03.x;
+    dK[1] = k_12.x;
+    dK[2] = k_12.y;
+    dK[3] = k_03.y;
 }
 
 // RK4 on a float-pair state (X = x^mu, K = k^mu), accelerations in float.
@@ -412,56 +457,19 @@ __device__ __forceinline__ void pair_state_update(const f2 X[4], const f2 K[4], 
 // along the 1000 M approach from the camera.  a1 = acceleration at X, K.
 __device__ __forceinline__ void rk4_step_pair(const f2 X[4], const f2 K[4], const float a1[4], float dt, float a,
                                               f2 Xo[4], f2 Ko[4]) {
-    float x[4], k[4], t[8], a2[4], a3[4], a4[4];
+    float x[4], k[4], dXa[4], dK[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) { x[i] = X[i].hi; k[i] = K[i].hi; }
-    const float h = 0.5f * dt;
-#pragma unroll
-    for (int i = 0; i < 4; i++) { t[i] = x[i] + h * k[i]; t[4 + i] = k[i] + h * a1[i]; }
-    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a2[0], a2[1], a2[2], a2[3]);
-#pragma unroll
-    for (int i = 0; i < 4; i++) { t[i] = x[i] + h * (k[i] + h * a1[i]); t[4 + i] = k[i] + h * a2[i]; }
-    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a3[0], a3[1], a3[2], a3[3]);
-#pragma unroll
-    for (int i = 0; i < 4; i++) { t[i] = x[i] + dt * (k[i] + h * a2[i]); t[4 + i] = k[i] + dt * a3[i]; }
-    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a4[0], a4[1], a4[2], a4[3]);
-    const float c = dt * dt * (1.0f / 6.0f);
-    const float d = dt * (1.0f / 6.0f);
-    float dXa[4], dK[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        dXa[i] = c * (a1[i] + a2[i] + a3[i]);
-        dK[i] = d * (a1[i] + 2.0f * a2[i] + 2.0f * a3[i] + a4[i]);
-    }
+    rk4_stages_f32(x, k, a1, dt, a, dXa, dK);
     pair_state_update(X, K, dt, dXa, dK, Xo, Ko);
 }
 
 // The RK4 increments of one step in float, for a state held elsewhere in
 // higher precision: x, k the state rounded to float, a1 the acceleration
-// there.  The position increment is dt k + dXa with dXa = dt^2/6 (a1 + a2 +
-// a3) (the caller forms dt k in its own precision), dK = dt/6 (a1 + 2 a2 +
-// 2 a3 + a4) -- RK4_gen's combination (geodesics.py:317-336) written for
-// x'' = a(x, x').
+// there (rk4_stages_f32).
 __device__ __forceinline__ void rk4_increment_f32(const float x[4], const float k[4], const float a1[4], float dt,
                                                   float a, float dXa[4], float dK[4]) {
-    float t[8], a2[4], a3[4], a4[4];
-    const float h = 0.5f * dt;
-#pragma unroll
-    for (int i = 0; i < 4; i++) { t[i] = x[i] + h * k[i]; t[4 + i] = k[i] + h * a1[i]; }
-    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a2[0], a2[1], a2[2], a2[3]);
-#pragma unroll
-    for (int i = 0; i < 4; i++) { t[i] = x[i] + h * (k[i] + h * a1[i]); t[4 + i] = k[i] + h * a2[i]; }
-    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a3[0], a3[1], a3[2], a3[3]);
-#pragma unroll
-    for (int i = 0; i < 4; i++) { t[i] = x[i] + dt * (k[i] + h * a2[i]); t[4 + i] = k[i] + dt * a3[i]; }
-    kerr_accel(t[1], t[2], t[3], t[4], t[5], t[6], t[7], a, a4[0], a4[1], a4[2], a4[3]);
-    const float c = dt * dt * (1.0f / 6.0f);
-    const float d = dt * (1.0f / 6.0f);
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        dXa[i] = c * (a1[i] + a2[i] + a3[i]);
-        dK[i] = d * (a1[i] + 2.0f * a2[i] + 2.0f * a3[i] + a4[i]);
-    }
+    rk4_stages_f32(x, k, a1, dt, a, dXa, dK);
 }
 
 // radius_cal (geodesics.py:284-291): the KS radius the step rule uses
