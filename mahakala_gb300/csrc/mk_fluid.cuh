@@ -455,7 +455,7 @@ __device__ __forceinline__ FluidF32 fluid_frame_f32(const float prim[8], const K
     const float lU = l1 * U1 + l2 * U2 + l3 * U3;
     const float gamma = sqrt_approx(1.0f + ((U1 * U1 + U2 * U2 + U3 * U3) + f * lU * lU));
     const float ga_f = gamma * alpha * f;
-    const float uc0 = gamma / alpha;
+    const float uc0 = gamma * ((1.0f + f) * alpha);  // gamma / alpha with alpha = 1/sqrt(1 + f)
     const float uc1 = U1 - ga_f * l1, uc2 = U2 - ga_f * l2, uc3 = U3 - ga_f * l3;
     const float lu = uc0 + l1 * uc1 + l2 * uc2 + l3 * uc3;
     const float flu = f * lu;

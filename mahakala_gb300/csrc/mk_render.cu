@@ -323,7 +323,13 @@ __device__ __forceinline__ void emission_f32_at(const mk_snapshot_view &sv, cons
             float em = __fdividef(Ne * sc[ch].k_em * nusp * term * term, 2.0f * th2 * nup * nup) * __expf(-x3);
             if (X > 1.e12f || cut) em = 0.0f;
             const float bx = __fdividef(sc[ch].k_bx * nup, Th);
-            const float bden = bx < 2.e-3f ? bx / 24.f * (24.f + bx * (12.f + bx * (4.f + bx))) : expm1f(bx);
+            // expm1(bx) (series below 2e-3; at radio frequencies bx ~ 1e-9);
+            // a branch, so the library expm1f is not evaluated beside it
+            float bden;
+            if (bx < 2.e-3f)
+                bden = bx * (1.0f / 24.0f) * (24.f + bx * (12.f + bx * (4.f + bx)));
+            else
+                bden = expm1f(bx);
             // alpha nu' = (em nu'^2) / B_nu * nu' with B_nu = k_bnu nu'^3 / bden
             float ab = __fdividef(em * bden, sc[ch].k_bnu);
             em_out[ch] = isnan(em) ? 0.0f : em;
