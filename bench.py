@@ -46,6 +46,12 @@ FLOP_PER_EXTRA_NU = 41
 
 L2_FLUSH_BYTES = 256 << 20
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# each mixed-form kernel (phases A, B, C) on the 256x256 workload, from one
+# `ncu --set full` capture of
+# `python bench.py --precision mixed --steps 2 --warmup 3 --quick --serving 0`
+NCU_TRAFFIC_RENDER256 = {"A": 107.70e6 + 3.69e6, "B": 76.72e6 + 1.75e6, "C": 113.28e6 + 3.73e6}
+
 # FP64 FLOP (DFMA = 2) per point of the standalone sampling stage, from ncu's
 # DADD/DMUL/DFMA thread-instruction counters on fluid_scalars_kernel (64x64
 # camera over the 256^3-cell snapshot, 19 % of points inside it)
@@ -400,9 +406,8 @@ def sampling_stage(torch, model, spec, flush, stream, fp64_peak, rays_per_side=1
                      "frac": flops / t / fp64_peak, "flop_per_point": SAMPLING_FP64_FLOP_PER_POINT},
             "traffic": None,
             "note": "every point needs the metric, fluid frame and arccos in binary64 to return the reference's "
-                    "values, so the stage is FP64-pipe bound (ncu: 87.5 % FP64 pipe, 2.6 % DRAM; "
-                    "profiles/fluid_scalars_kernel_sampling64.md); FLOP per point from ncu's FP64 instruction "
-                    "counters on the 64x64 case"}
+                    "values, so the stage is FP64-pipe bound (ncu on the 64x64 case: 87.5 % FP64 pipe, 2.6 % DRAM); "
+                    "FLOP per point from ncu's FP64 instruction counters on the same case"}
 
 
 def run_vacuum(args):
@@ -593,7 +598,7 @@ def main():
                "ALU figure")
         if form == "fp64":
             kernels = [("render_fp64_kernel", "fp64", r["steps"] * FLOP_PER_STEP + r["samples"] * per_sample,
-                        r["t_phase"][0], peak64)]
+                        r["t_phase"][0], peak64, None)]
         else:
             to64, back32, steps64 = r["split"]
             stb, smb = r["work_b"] if r["work_b"] else (steps64, r["samples64"])
@@ -603,22 +608,30 @@ def main():
             zone = stb * FLOP_PER_STEP + smb * per_sample
             fc = stc * FLOP_PER_STEP + smc * per_sample
             if form == "mixed":  # float accelerations and emission, float-pair state, compensated sums
-                kb = ("render_zone_kernel (phase B: near the hole and after; beside C)", "fp32", zone, tB, peak32)
-                kc = ("render_f32_kernel (phase C: parked outbound rays; beside B)", "fp32", fc, tC, peak32)
+                kb = ("render_zone_kernel (phase B: near the hole and after; beside C)", "fp32", zone, tB, peak32, "B")
+                kc = ("render_f32_kernel (phase C: parked outbound rays; beside B)", "fp32", fc, tC, peak32, "C")
             else:
-                kb = ("render_fp64_kernel (phase B, near the hole)", "fp64", zone, tB, peak64)
-                kc = ("render_f32_kernel (phase C)", "fp32", fc, tC, peak32)
-            kernels = [("render_f32_kernel (phase A)", "fp32", fa, tA, peak32), kb, kc]
+                kb = ("render_fp64_kernel (phase B, near the hole)", "fp64", zone, tB, peak64, None)
+                kc = ("render_f32_kernel (phase C)", "fp32", fc, tC, peak32, None)
+            kernels = [("render_f32_kernel (phase A)", "fp32", fa, tA, peak32, "A"), kb, kc]
+        measured = (NCU_TRAFFIC_RENDER256 if form == "mixed" and args.workload == "render256" and not args.resolution
+                    else {})
         table = [{"kernel": k, "bound": b, "flop": fl, "ms": 1e3 * t, "achieved": fl / t / 1e12 if t else None,
-                  "peak": pk / 1e12, "frac": fl / t / pk if t else None} for k, b, fl, t, pk in kernels]
+                  "peak": pk / 1e12, "frac": fl / t / pk if t else None,
+                  "traffic": measured.get(tag) if tag else None}
+                 for k, b, fl, t, pk, *rest in kernels for tag in [rest[0] if rest else None]]
         top = max(table, key=lambda e: e["ms"])
         out = {"bound": top["bound"], "achieved": top["achieved"], "peak": top["peak"], "unit": "TFLOP/s",
-               "frac": top["frac"], "traffic": None, "kernel": top["kernel"], "flop_per_launch": top["flop"],
+               "frac": top["frac"], "traffic": top["traffic"], "kernel": top["kernel"], "flop_per_launch": top["flop"],
                "kernel_ms": top["ms"], "peak_source": src, "kernels": table,
                "peak_fp32_tflops": peak32 / 1e12, "peak_fp64_tflops": peak64 / 1e12}
+        if top["traffic"] is not None:
+            out["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
+                                     "kernel on this workload (bytes per launch); the kernels are ALU- and "
+                                     "latency-bound, the gathers hit L1/L2")
         if form == "fp64":
             out["traffic_note"] = ("ncu on the 192x192 case: 242 MB DRAM read per launch; the kernel is "
-                                   "FP64-pipe bound (profiles/render_fp64_kernel_render192.md)")
+                                   "FP64-pipe bound (71 % FP64 pipe, 0.04 % DRAM)")
         else:
             out["note"] = ("phase B runs the serial chain of its longest ray (zone_run_max steps) on one warp "
                            "per sub-partition: latency-bound, not throughput-bound")

@@ -389,7 +389,7 @@ void orc_shadow_bisection(const double *cosang, const double *sinang, int n, dou
 }
 
 /* ------------------------------------------------------------------ */
-/* BASELINE vacuum step policy (not in the reference): h = 0.05 r       */
+/* fixed-fraction vacuum step policy (not in the reference): h = 0.05 r */
 /* clamped to [hmin, hmax], captured at r < cap*r_h, escaped at r >     */
 /* r_esc once r increases, at most N steps.                              */
 /* ------------------------------------------------------------------ */
