@@ -92,8 +92,8 @@ static int phase_mark(cudaStream_t st, int i, int from = -1) {
 // A second stream per host thread and device, with the two events that fork
 // it from and join it back to the caller's stream within one render.  Reused
 // across calls: a wait takes the event's latest record at the time it is
-// enqueued.  Created on a thread's first mixed-form render (an eager call;
-// a render captured into a graph records its fork and join as graph edges).
+// enqueued.  Created on a thread's first mixed-form render; a render
+// captured into a graph records its fork and join as graph edges.
 struct SideStream {
     cudaStream_t s = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
@@ -106,9 +106,16 @@ static int side_stream(SideStream **out) {
     MK_REQUIRE(dev >= 0 && dev < 64, MK_ERR_LIMIT, "side stream: device ordinal %d not supported", dev);
     SideStream &x = t_side[dev];
     if (!x.s) {
-        MK_CUDA(cudaStreamCreateWithFlags(&x.s, cudaStreamNonBlocking));
-        MK_CUDA(cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming));
-        MK_CUDA(cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming));
+        // the first call may come inside a stream capture: create the stream
+        // and events under the relaxed capture mode, then restore the caller's
+        cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+        MK_CUDA(cudaThreadExchangeStreamCaptureMode(&mode));
+        const cudaError_t e1 = cudaStreamCreateWithFlags(&x.s, cudaStreamNonBlocking);
+        const cudaError_t e2 = e1 == cudaSuccess ? cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming) : e1;
+        const cudaError_t e3 = e2 == cudaSuccess ? cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming) : e2;
+        MK_CUDA(cudaThreadExchangeStreamCaptureMode(&mode));
+        if (e3 != cudaSuccess) x.s = nullptr;
+        MK_CUDA(e3);
     }
     *out = &x;
     return MK_OK;

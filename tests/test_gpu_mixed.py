@@ -149,3 +149,42 @@ def test_phase_events_and_zone_switch(cuda, medium_model):
     a, b = prep.images[0][0].cpu().numpy(), ref.images[0][0].cpu().numpy()
     assert np.all(np.isfinite(a)) and a.max() > 0
     assert metrics.flux_rel_err(a, b) <= 1e-2
+
+
+def test_mixed_render_captured_from_fresh_thread(cuda, medium_model):
+    """A mixed-form render captured into a CUDA graph on a host thread that
+    has not rendered before -- its side stream (phase C runs beside phase B
+    on it) is created inside the capture -- replays to the eager image, bit
+    for bit."""
+    import threading
+
+    import torch
+
+    from mahakala_gb300.images import PreparedRender, RenderRequest
+    kw = dict(camera_inclination=17.0, resolution=32, fov=50.0, max_nsteps=8192)
+    eager = PreparedRender([RenderRequest(medium_model, **kw)], precision="mixed")
+    eager.launch()
+    torch.cuda.synchronize()
+    ref = eager.images[0].cpu().numpy()
+    out = {}
+
+    def worker():
+        try:
+            prep = PreparedRender([RenderRequest(medium_model, **kw)], precision="mixed")
+            s = torch.cuda.Stream()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=s):
+                prep.launch(s)
+            for _ in range(2):
+                g.replay()
+            torch.cuda.synchronize()
+            out["img"] = prep.images[0].cpu().numpy()
+        except Exception as e:  # reported on the test's thread
+            out["err"] = e
+
+    t = threading.Thread(target=worker)
+    t.start()
+    t.join()
+    assert "err" not in out, out.get("err")
+    assert np.array_equal(out["img"], ref, equal_nan=True)
+    assert ref.max() > 0
