@@ -115,8 +115,7 @@ __device__ __forceinline__ void kerr_accel_f32(float x, float y, float z, float 
     const float kk = 0.5f * (x * x + y * y + zz - aa);
     const float Q = kk * kk + aa * zz;
     const float iq = inv_sqrt(Q);
-    const float q = Q * iq;                  // sqrt(kk^2 + a^2 z^2)
-    const float rr = q + kk;
+    const float rr = fmaf(Q, iq, kk);        // sqrt(kk^2 + a^2 z^2) + kk
     const float ir = inv_sqrt(rr);
     const float r = rr * ir;
     const float i2rq = 0.5f * ir * iq;       // 1 / (2 r q)
@@ -128,15 +127,14 @@ __device__ __forceinline__ void kerr_accel_f32(float x, float y, float z, float 
     const float iden = ID.x, ira = ID.y;
     const float2 RXY = __fmul2_rn(both(rr * i2rq), XY);  // (dr/dx, dr/dy)
     const float rz = rra * z * i2rq;
-    const float rrr = rr * r;
-    const float f = 2.0f * rrr * iden;
-    const float c1 = 3.0f * ir - 4.0f * rrr * iden;
+    const float f = 2.0f * (rr * r * iden);
+    const float c1 = fmaf(-2.0f, f, 3.0f * ir);  // 3/r - 4 r^3/den
     // (l1, l2) = (r x + a y, r y - a x) / (r^2 + a^2); (g1, g2) = (xy - 2 r l) / (r^2 + a^2)
     const float2 L12 = __fmul2_rn(__ffma2_rn(both(r), XY, __fmul2_rn(both(a), pair(y, -x))), both(ira));
     const float l3 = z * ir;
     const float2 G12 = __fmul2_rn(__ffma2_rn(both(-2.0f * r), L12, XY), both(ira));
     const float rira = r * ira, aira = a * ira;
-    const float h = z * ir * ir;
+    const float h = l3 * ir;
     const float Dr = k1 * RXY.x + k2 * RXY.y + k3 * rz;
     const float fc = f * c1;
     const float ft = f * (2.0f * aa * z * iden);
