@@ -645,6 +645,8 @@ def main():
                 "accepted_steps": r["steps"], "samples": r["samples"], "steps_per_ray": r["steps"] / rays,
                 "rays_to_fp64": to64, "rays_back_to_fp32": back32, "steps_in_fp64": steps64,
                 "zone_run_max": r["zone_run_max"],
+                "phase_b_steps_samples": list(r["work_b"]) if r["work_b"] else None,
+                "phase_c_steps_samples": list(r["work_c"]) if r["work_c"] else None,
                 "max_step_optical_depth": r["max_tau"],
                 "flux_jy": [float(x) for x in np.atleast_1d(image_flux_jy(r["image"], spec.fov, spec.distance_cm,
                                                                          L_unit))],
