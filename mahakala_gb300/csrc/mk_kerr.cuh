@@ -14,7 +14,12 @@
 // and with D = k^c d_c (spatial directional derivative), lv = l.k,
 //   F_nu = -[Df l_nu lv + f (Dl_nu lv + l_nu Dl.k)] + 1/2 d_nu f lv^2 + f lv (d_nu l.k)
 //   accel^mu = g^{mu nu} F_nu,
-// which equals -Gamma^mu_ab k^a k^b, the quantity rhs() returns.
+// which equals -Gamma^mu_ab k^a k^b, the quantity rhs() returns.  With
+// F_0 = -(Df lv + f Dl.k) the spatial components read
+//   F_i = l_i F_0 + f lv (d_i l.k - D l_i) + 1/2 d_i f lv^2,
+// and every position derivative goes through d r: d l1 = g1 d r + (r, a, 0)
+// / (rr + a^2), d l2 = g2 d r + (-a, r, 0) / (rr + a^2), d l3 = -(l3/r) d r +
+// (0, 0, 1/r), so D and d_i . k need k.d r, not the nine components d_c l_i.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -92,17 +97,12 @@ __device__ __forceinline__ KerrPoint<T> kerr_point(T x, T y, T z, T a) {
     return m;
 }
 
-// The FP32 geodesic acceleration (mixed-precision phases).  Same
-// contraction as the generic form below, rearranged for fewer
-// instructions: f and l_i depend on position through r and through explicit
-// x, y, z terms -- grad l1 = g1 grad r + (r, a, 0)/(r^2 + a^2), grad l2 =
-// g2 grad r + (-a, r, 0)/(r^2 + a^2), grad l3 = -h grad r + (0, 0, 1/r) --
-// so the derivatives along k (D = k . grad) and the sums d = sum_i k_i
-// grad l_i come from k . grad r without the nine gradient components, and
-// F_i = l_i F_0 + f (k.l) (d_i - D l_i) + f_i (k.l)^2 / 2.  The x and y
-// components go through paired FP32 instructions (two lanes of one
-// instruction, each rounded as its scalar twin).  Equal to the generic form
-// to float rounding.
+// The FP32 geodesic acceleration (mixed-precision phases): the contraction
+// of the generic form below (derivatives along k from k . grad r, F_i = l_i
+// F_0 + f (k.l) (d_i - D l_i) + f_i (k.l)^2 / 2), with the x and y
+// components on paired FP32 instructions (two lanes of one instruction,
+// each rounded as its scalar twin).  Equal to the generic form to float
+// rounding.
 __device__ __forceinline__ float2 pair(float u, float v) { return make_float2(u, v); }
 __device__ __forceinline__ float2 both(float u) { return make_float2(u, u); }
 
@@ -178,13 +178,15 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
     if constexpr (std::is_same<T, float>::value) {
         kerr_accel_f32(x, y, z, k0, k1, k2, k3, a, a0, a1, a2, a3, m);
     } else {
+        // the same contraction as kerr_accel_f32 (derivatives along k from
+        // k . grad r, F_i = l_i F0 + f (k.l)(d_i - D l_i) + f_i (k.l)^2/2),
+        // each operation in T
         const T aa = a * a;
         const T zz = z * z;
         const T kk = T(0.5f) * (x * x + y * y + zz - aa);
         const T Q = kk * kk + aa * zz;
         const T iq = inv_sqrt(Q);
-        const T q = Q * iq;                      // sqrt(kk^2 + a^2 z^2)
-        const T rr = q + kk;
+        const T rr = Q * iq + kk;                 // sqrt(kk^2 + a^2 z^2) + kk
         const T ir = inv_sqrt(rr);
         const T r = rr * ir;
         const T i2rq = T(0.5f) * ir * iq;         // 1 / (2 r q)
@@ -195,15 +197,11 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
         const T iden = rra * inv2;
         const T ira = den * inv2;
 
-        const T rx = rr * x * i2rq;
-        const T ry = rr * y * i2rq;
+        const T c = rr * i2rq;
+        const T rx = c * x, ry = c * y;           // dr/dx, dr/dy
         const T rz = rra * z * i2rq;
-
-        const T f = T(2.0f) * rr * r * iden;
-        const T c1 = T(3.0f) * ir - T(4.0f) * rr * r * iden;
-        const T fx = f * (c1 * rx);
-        const T fy = f * (c1 * ry);
-        const T fz = f * (c1 * rz - T(2.0f) * aa * z * iden);
+        const T f = T(2.0f) * (rr * r * iden);
+        const T c1 = T(3.0f) * ir - T(2.0f) * f;
 
         const T l1 = (r * x + a * y) * ira;
         const T l2 = (r * y - a * x) * ira;
@@ -212,29 +210,30 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
         const T g1 = (x - tr * l1) * ira;
         const T g2 = (y - tr * l2) * ira;
         const T rira = r * ira, aira = a * ira;
-        const T l1x = g1 * rx + rira, l1y = g1 * ry + aira, l1z = g1 * rz;
-        const T l2x = g2 * rx - aira, l2y = g2 * ry + rira, l2z = g2 * rz;
-        const T h = z * ir * ir;
-        const T l3x = -h * rx, l3y = -h * ry, l3z = ir - h * rz;
+        const T h = l3 * ir;
+
+        const T Dr = k1 * rx + k2 * ry + k3 * rz;
+        const T fc = f * c1;
+        const T ft = f * (T(2.0f) * aa * z * iden);
+        const T fx = fc * rx, fy = fc * ry, fz = fc * rz - ft;
+        const T Df = fc * Dr - ft * k3;
+        const T u1 = rira * k1, u2 = rira * k2, v1 = aira * k1, v2 = aira * k2;
+        const T Dl1 = g1 * Dr + (u1 + v2);
+        const T Dl2 = g2 * Dr + (u2 - v1);
+        const T Dl3 = ir * k3 - h * Dr;
+        const T G = g1 * k1 + g2 * k2 - h * k3;
+        const T dlx = rx * G + (u1 - v2);
+        const T dly = ry * G + (v1 + u2);
+        const T dlz = rz * G + ir * k3;
 
         const T lv = k0 + l1 * k1 + l2 * k2 + l3 * k3;
-        const T Df = k1 * fx + k2 * fy + k3 * fz;
-        const T Dl1 = k1 * l1x + k2 * l1y + k3 * l1z;
-        const T Dl2 = k1 * l2x + k2 * l2y + k3 * l2z;
-        const T Dl3 = k1 * l3x + k2 * l3y + k3 * l3z;
         const T Dlv = Dl1 * k1 + Dl2 * k2 + Dl3 * k3;
-        const T dlx = l1x * k1 + l2x * k2 + l3x * k3;
-        const T dly = l1y * k1 + l2y * k2 + l3y * k3;
-        const T dlz = l1z * k1 + l2z * k2 + l3z * k3;
-
-        const T Dflv = Df * lv;
-        const T fDlv = f * Dlv;
-        const T half_lv2 = T(0.5f) * lv * lv;
         const T flv = f * lv;
-        const T F0 = -(Dflv + fDlv);
-        const T F1 = -(Dflv * l1 + f * (Dl1 * lv) + l1 * fDlv) + fx * half_lv2 + flv * dlx;
-        const T F2 = -(Dflv * l2 + f * (Dl2 * lv) + l2 * fDlv) + fy * half_lv2 + flv * dly;
-        const T F3 = -(Dflv * l3 + f * (Dl3 * lv) + l3 * fDlv) + fz * half_lv2 + flv * dlz;
+        const T hl = T(0.5f) * lv * lv;
+        const T F0 = -(Df * lv + f * Dlv);
+        const T F1 = l1 * F0 + flv * (dlx - Dl1) + fx * hl;
+        const T F2 = l2 * F0 + flv * (dly - Dl2) + fy * hl;
+        const T F3 = l3 * F0 + flv * (dlz - Dl3) + fz * hl;
         const T lF = -F0 + l1 * F1 + l2 * F2 + l3 * F3;
         const T flF = f * lF;
         a0 = -F0 + flF;
