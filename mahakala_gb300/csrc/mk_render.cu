@@ -20,18 +20,22 @@
 //
 // Precision forms:
 //   MK_FP64  one launch, every operation in FP64 (the reference's x64).
-//   MK_MIXED two launches on the caller's stream:
+//   MK_MIXED three launches, A on the caller's stream, then B on it and C
+//   on a side stream forked after A and joined back after C:
 //     A  FP32 from the camera.  A ray whose radius drops below R_FP64 (3 M),
 //        or that moves inward inside R_TURN (6 M, where photon-ring rays
-//        reach their turning points), is handed to a queue (FP64 record);
-//     B  that queue (render_zone_kernel): the float-pair state is
+//        reach their turning points), is handed to the near-hole queue; a
+//        ray moving outward past R_TURN is parked in the FP32 queue (records
+//        in binary64);
+//     B  the near-hole queue (render_zone_kernel): the float-pair state is
 //        renormalised to null in binary64 on entry, at each radial turning
 //        point and when the ray leaves R_TURN outward; the kernel carries the
-//        ray on to its end.
+//        ray on to its end;
+//     C  the FP32 queue (render_f32_kernel over the queue), beside B: the
+//        two share no ray and no counter.
 //   MK_MIXED_STRICT: phase B integrates the near-hole geodesic entirely in
 //   binary64 (render_fp64_kernel over the queue) and parks rays leaving it
-//   for a third launch (phase C, FP32); MK_MIXED_DF: the same in
-//   double-float pairs.
+//   for phase C, after it; MK_MIXED_DF: the same in double-float pairs.
 //   Splitting by precision keeps each warp uniform: on a part whose FP64
 //   rate is 1/64 of FP32, one FP64 lane would stall the other 31.  The
 //   intensity accumulates with a compensated (Kahan) FP32 sum and the

@@ -149,18 +149,18 @@ class PreparedRender:
         return int(w[_lib.MK_WS_STEPS]), int(w[_lib.MK_WS_SAMPLES])
 
     def precision_split(self):
-        """(rays handed to FP64, rays handed back to FP32, steps taken in
-        FP64) of the last mixed-form launch (syncs)."""
+        """(rays handed to the near-hole phase, rays that left it outward,
+        steps taken near the hole) of the last mixed-form launch (syncs)."""
         w = self.ws[:32].cpu()
         return int(w[_lib.MK_WS_TO_FP64]), int(w[_lib.MK_WS_TO_FP32]), int(w[_lib.MK_WS_STEPS_FP64])
 
     def samples_fp64(self):
-        """In-snapshot samples taken in the FP64 phase of the last
-        mixed-form launch (syncs)."""
+        """In-snapshot samples taken near the hole in the last mixed-form
+        launch (syncs)."""
         return int(self.ws[:32].cpu()[_lib.MK_WS_SAMPLES_FP64])
 
     def phase_b_work(self):
-        """(steps, samples) the last MK_MIXED launch's second kernel took
+        """(steps, samples) the last MK_MIXED launch's near-hole kernel took
         (syncs)."""
         w = self.ws[:32].cpu()
         return int(w[_lib.MK_WS_STEPS_B]), int(w[_lib.MK_WS_SAMPLES_B])
