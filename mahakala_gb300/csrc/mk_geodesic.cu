@@ -39,9 +39,12 @@ integrate_reference_kernel(const double *__restrict__ s0, int64_t npx, double a,
     for (int i = 0; i < 8; i++) s[i] = s0[8 * p + i];
     const double reh = radius_eh(a);
     int K = N, why = MK_RAY_MAXSTEPS;
+    // a step's dt is the previous step's dtn (the same radius_cal of the same
+    // state), carried instead of recomputed
+    int w0;
+    double dt = reference_dt(radius_cal(s[1], s[2], s[3], a), reh, div, tol, w0);
     for (int j = 0; j < N; j++) {
-        int w0, w1;
-        const double dt = reference_dt(radius_cal(s[1], s[2], s[3], a), reh, div, tol, w0);
+        int w1;
         rk4_step(s, dt, a, nw);
         const double dtn = reference_dt(radius_cal(nw[1], nw[2], nw[3], a), reh, div, tol, w1);
         if (dtn == 0.0) {
@@ -61,6 +64,8 @@ integrate_reference_kernel(const double *__restrict__ s0, int64_t npx, double a,
         if (dts) dts[(int64_t)j * npx + p] = dt;
 #pragma unroll
         for (int i = 0; i < 8; i++) s[i] = nw[i];
+        dt = dtn;
+        w0 = w1;
     }
     Kout[p] = K;
     why_out[p] = why;
@@ -122,12 +127,14 @@ shadow_pass_kernel(const double *__restrict__ ca, const double *__restrict__ sa,
     const double reh = radius_eh(a);
     int K = N, best = -1;
     double best_dt = -INFINITY, r_prev = nan(""), rb = nan(""), rk = nan(""), rl = nan("");
+    int w0;
+    double r_here = radius_cal(s[1], s[2], s[3], a);
+    double dt = reference_dt(r_here, reh, 40.0, 1e-2, w0);  // carried from step to step, as above
     for (int j = 0; j < N; j++) {
-        int w0, w1;
-        const double r_here = radius_cal(s[1], s[2], s[3], a);
-        const double dt = reference_dt(r_here, reh, 40.0, 1e-2, w0);
+        int w1;
         rk4_step(s, dt, a, nw);
-        const double dtn = reference_dt(radius_cal(nw[1], nw[2], nw[3], a), reh, 40.0, 1e-2, w1);
+        const double r_next = radius_cal(nw[1], nw[2], nw[3], a);
+        const double dtn = reference_dt(r_next, reh, 40.0, 1e-2, w1);
         if (dtn == 0.0) {
             K = j;
             rk = r_prev;   // row K-1
@@ -139,6 +146,8 @@ shadow_pass_kernel(const double *__restrict__ ca, const double *__restrict__ sa,
         if (j == N - 1) rl = r_here;  // row N-1 = state before step N-1
 #pragma unroll
         for (int i = 0; i < 8; i++) s[i] = nw[i];
+        r_here = r_next;
+        dt = dtn;
     }
     Kout[p] = K;
     best_out[p] = best;
