@@ -982,11 +982,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
         }
         if (active) {
             const mk_request &R = reqs[rq];
-            // re-read the request constants every step: an address the
-            // compiler cannot hoist keeps them out of the loop's registers
-            const ReqF32 *qp = s_req + rq;
-            asm volatile("" : "+l"(qp));
-            const ReqF32 &Q = *qp;
+            const ReqF32 &Q = s_req[rq];  // the request's constants, from shared memory
             f2 Xn[4], Kn[4];
             float dn[4];
             rk4_step_pair(X, K, d1, dt, Q.a, Xn, Kn);
