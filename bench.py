@@ -700,7 +700,10 @@ def main():
                 "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
         "serving": serving,
         "sampling_stage": sampling,
-        "gpu_launches": args.steps * {"fp64": 1}.get(head, 3),
+        # per render: FP64 one kernel; mixed forms A, B, C, plus the camera-state
+        # kernel when the launch exceeds one wave of phase A at 4 blocks per SM
+        "gpu_launches": args.steps * (1 if head == "fp64" else
+                                      3 + int(rays > _lib.load().mk_device_sm_count() * 4 * 128)),
         "phase_ms": {f: [1e3 * t for t in res[f]["t_phase"]] for f in forms},
         "clocks": clocks,
         "snapshot_build_s": t_gen,

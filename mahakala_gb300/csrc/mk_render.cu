@@ -42,6 +42,8 @@
 //   transmission product in FP32; both move to FP64 with the ray.
 #include <string.h>
 
+#include <algorithm>
+
 #include "mk_common.cuh"
 #include "mk_dd.cuh"
 #include "mk_fluid.cuh"
@@ -51,7 +53,12 @@ namespace mk {
 constexpr int RENDER_THREADS = 128;
 constexpr double R_FP64 = 3.0;
 constexpr double R_TURN = 6.0;
-enum : int { F32_HANDOFF = 1, F32_PARK = 2 };
+// F32_RENULL (the FP32 queue): renormalise each resumed ray to null in
+// binary64 -- for rays leaving the binary64 near-hole phase of
+// MK_MIXED_STRICT / MK_MIXED_DF; MK_MIXED's parked rays come from phase A's
+// float-pair state, null to well under half a float ulp of k^t (the images
+// were bit-identical with and without), and skip it
+enum : int { F32_HANDOFF = 1, F32_PARK = 2, F32_RENULL = 4 };
 
 // rays per warp in the mixed form's FP64 phase (mk_set_tuning
 // "fp64_rays_per_warp"): 32 fills every lane; fewer rays per warp shorten
@@ -889,6 +896,29 @@ render_zone_kernel(const mk_request *__restrict__ reqs, const mk_snapshot_view *
 }
 
 
+// Initial states of every camera ray of a launch, in FP64 (camera_ray),
+// for mixed-form launches larger than one wave of phase A: there each thread
+// of phase A takes a new ray many times, and the ~270 FP64 instructions of a
+// camera ray, run for whichever lanes refill in a given step, held the
+// whole warp on the sub-partition's FP64 unit each time.  Here they run
+// once per ray, fully parallel, and phase A loads 64 bytes instead.
+__global__ void __launch_bounds__(RENDER_THREADS)
+camera_states_kernel(const mk_request *__restrict__ reqs, int nreq, long long total, const mk_job *job,
+                     double *__restrict__ out) {
+    if (job) {
+        nreq = job->nreq;
+        total = job->total_rays;
+    }
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int rq = find_request(reqs, nreq, p);
+        double s[8];
+        camera_ray(reqs[rq].camera, p - reqs[rq].ray_offset, s);
+#pragma unroll
+        for (int i = 0; i < 8; i++) out[8 * p + i] = s[i];
+    }
+}
+
 // FP32 render phase.  SRC_CAMERA: mixed-form phase A from the camera; mode
 // F32_HANDOFF hands rays near the hole to the near-hole queue, F32_PARK
 // parks rays leaving the photon-ring region outward in the FP32 queue.
@@ -899,7 +929,7 @@ template <int SRC, int MINB>
 __global__ void __launch_bounds__(RENDER_THREADS, MINB)
 render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
                   const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64, RayRecord *q32,
-                  long long capacity, const mk_job *job, int mode) {
+                  long long capacity, const mk_job *job, int mode, const double *__restrict__ cam) {
     if (job) {
         nreq = job->nreq;
         total_camera = job->total_rays;
@@ -929,7 +959,12 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 ray = idx;
                 rq = find_request(reqs, nreq, ray);
                 pix = ray - reqs[rq].ray_offset;
-                camera_ray(reqs[rq].camera, pix, s64);
+                if (cam) {  // precomputed by camera_states_kernel
+                #pragma unroll
+                    for (int i = 0; i < 8; i++) s64[i] = cam[8 * ray + i];
+                } else {
+                    camera_ray(reqs[rq].camera, pix, s64);
+                }
                 steps = nsamples = 0;
                 max_tau = 0.0f;
 #pragma unroll
@@ -950,7 +985,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 nsamples = q.nsamples;
                 rq = q.rq;
                 pix = ray - reqs[rq].ray_offset;
-                renull_fp64(s64, reqs[rq].camera.bhspin);
+                if (mode & F32_RENULL) renull_fp64(s64, reqs[rq].camera.bhspin);
             }
             const mk_request &R = reqs[rq];
             if (rq >= MK_MAX_REQUESTS_MIXED) {  // beyond the launch's request table
@@ -1100,16 +1135,34 @@ extern "C" int mk_set_tuning(const char *name, int64_t value) {
     MK_REQUIRE(false, MK_ERR_ARG, "mk_set_tuning: unknown parameter '%s'", name);
 }
 
+// Scratch of a launch: the counter header, then (mixed forms) the two ray
+// queues, then -- for launches larger than one wave of phase A at 4 blocks
+// per SM -- the precomputed camera states (64 bytes a ray).  A workspace of
+// the size without them (ws_base) still renders: phase A then computes the
+// camera states itself.
+static bool mixed_form(int32_t precision) {
+    return precision == MK_MIXED || precision == MK_MIXED_DF || precision == MK_MIXED_STRICT;
+}
+static size_t ws_base(int64_t rays, int32_t precision) {
+    return mixed_form(precision) ? WS_HEADER + 2 * (size_t)rays * sizeof(RayRecord) : WS_HEADER;
+}
+static bool camera_precompute(int64_t rays, int32_t precision) {
+    return mixed_form(precision) && rays > (int64_t)device_sm_count() * 4 * RENDER_THREADS;
+}
+
+}  // namespace mk
+
 extern "C" size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision) {
     if (total_rays < 0) return 0;
-    if (precision == MK_MIXED || precision == MK_MIXED_DF || precision == MK_MIXED_STRICT)
-        return WS_HEADER + 2 * (size_t)total_rays * sizeof(RayRecord);
-    return WS_HEADER;
+    return mk::ws_base(total_rays, precision) +
+           (mk::camera_precompute(total_rays, precision) ? 8 * sizeof(double) * (size_t)total_rays : 0);
 }
+
+namespace mk {
 
 static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays, int64_t max_rays,
                          const mk_job *job_dev, const mk_snapshot_view *snaps_dev, int32_t precision,
-                         void *workspace_dev, cudaStream_t st) {
+                         void *workspace_dev, size_t workspace_bytes, cudaStream_t st) {
     MK_CUDA(cudaMemsetAsync(workspace_dev, 0, WS_HEADER, st));
     if (max_rays == 0) return MK_OK;
     RenderWorkspace *ws = (RenderWorkspace *)workspace_dev;
@@ -1126,6 +1179,16 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     RayRecord *q64 = (RayRecord *)((char *)workspace_dev + WS_HEADER);
     RayRecord *q32 = q64 + max_rays;
     const long long cap = (long long)max_rays;
+    double *cam = nullptr;
+    if (camera_precompute(max_rays, precision) &&
+        workspace_bytes >= ws_base(max_rays, precision) + 8 * sizeof(double) * (size_t)max_rays) {
+        cam = (double *)(q32 + max_rays);
+        const int64_t grid = std::min<int64_t>((max_rays + RENDER_THREADS - 1) / RENDER_THREADS,
+                                               (int64_t)device_sm_count() * 16);
+        camera_states_kernel<<<(unsigned)grid, RENDER_THREADS, 0, st>>>(reqs_dev, nreq, (long long)total_rays,
+                                                                         job_dev, cam);
+        MK_LAUNCHED("camera_states_kernel");
+    }
     int f32_blocks = g_f32_blocks;
     if (f32_blocks == 0)
         f32_blocks = max_rays > (int64_t)device_sm_count() * 4 * RENDER_THREADS ? 5 : 4;
@@ -1135,32 +1198,35 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     if (f32_blocks == 5)
         render_f32_kernel<SRC_CAMERA, 5>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 5>, 5), max_rays), RENDER_THREADS, 0,
-               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode);
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode, cam);
     else if (f32_blocks == 4)
         render_f32_kernel<SRC_CAMERA, 4>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 4>, 1), max_rays), RENDER_THREADS, 0,
-               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode);
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode, cam);
     else
         render_f32_kernel<SRC_CAMERA, 3>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 3>, 2), max_rays), RENDER_THREADS, 0,
-               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode);
+               st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode, cam);
     MK_LAUNCHED("render_f32_kernel (camera)");
     if ((rc = phase_mark(st, 1)) != MK_OK) return rc;
     // The FP32 continuation over the FP32 queue; its size is only known on
     // the device, so the grid is persistent.
+    // MK_MIXED's FP32 queue holds parked phase-A rays; the other mixed forms'
+    // hold the near-hole phase's exits
+    const int qmode = precision == MK_MIXED ? 0 : F32_RENULL;
     auto launch_f32_queue = [&](cudaStream_t s) {
         if (f32_blocks == 5)
             render_f32_kernel<SRC_QUEUE, 5>
                 <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 5>, 6), max_rays), RENDER_THREADS, 0,
-                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
+                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, qmode, nullptr);
         else if (f32_blocks == 4)
             render_f32_kernel<SRC_QUEUE, 4>
                 <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 4>, 3), max_rays), RENDER_THREADS, 0,
-                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
+                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, qmode, nullptr);
         else
             render_f32_kernel<SRC_QUEUE, 3>
                 <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 3>, 4), max_rays), RENDER_THREADS, 0,
-                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, 0);
+                   s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, qmode, nullptr);
     };
     // The near-hole queue: persistent grids, small blocks, so the few rays
     // near the hole spread over every SM sub-partition (they are
@@ -1212,14 +1278,14 @@ extern "C" int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     MK_REQUIRE(nreq > 0 && nsnap > 0 && total_rays >= 0, MK_ERR_ARG, "mk_render: bad sizes");
     MK_REQUIRE(precision >= MK_FP64 && precision <= MK_MIXED_STRICT, MK_ERR_ARG, "mk_render: unknown precision %d",
                (int)precision);
-    const size_t need = mk_render_workspace_bytes(total_rays, precision);
+    const size_t need = mk::ws_base(total_rays, precision);
     MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render: workspace of %zu bytes, need %zu",
                workspace_bytes, need);
     MK_REQUIRE(precision == MK_FP64 || nreq <= MK_MAX_REQUESTS_MIXED, MK_ERR_LIMIT,
                "mk_render: %d requests in one mixed-form launch, at most %d", (int)nreq, MK_MAX_REQUESTS_MIXED);
     MK_REQUIRE(((uintptr_t)workspace_dev & 15) == 0, MK_ERR_ARG, "mk_render: workspace not 16-byte aligned");
     return mk::launch_render(reqs_dev, nreq, total_rays, total_rays, nullptr, snaps_dev, precision, workspace_dev,
-                             mk::as_stream(stream));
+                             workspace_bytes, mk::as_stream(stream));
 }
 
 extern "C" int mk_render_job(const mk_job *job_dev, const mk_request *reqs_dev, const mk_snapshot_view *snaps_dev,
@@ -1229,12 +1295,12 @@ extern "C" int mk_render_job(const mk_job *job_dev, const mk_request *reqs_dev, 
     MK_REQUIRE(max_rays >= 0, MK_ERR_ARG, "mk_render_job: negative max_rays");
     MK_REQUIRE(precision >= MK_FP64 && precision <= MK_MIXED_STRICT, MK_ERR_ARG,
                "mk_render_job: unknown precision %d", (int)precision);
-    const size_t need = mk_render_workspace_bytes(max_rays, precision);
+    const size_t need = mk::ws_base(max_rays, precision);
     MK_REQUIRE(workspace_bytes >= need, MK_ERR_ARG, "mk_render_job: workspace of %zu bytes, need %zu",
                workspace_bytes, need);
     MK_REQUIRE(((uintptr_t)workspace_dev & 15) == 0, MK_ERR_ARG, "mk_render_job: workspace not 16-byte aligned");
     return mk::launch_render(reqs_dev, 1, 0, max_rays, job_dev, snaps_dev, precision, workspace_dev,
-                             mk::as_stream(stream));
+                             workspace_bytes, mk::as_stream(stream));
 }
 
 // the allocation-free entry point sizes its static workspace from these

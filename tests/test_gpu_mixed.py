@@ -188,3 +188,29 @@ def test_mixed_render_captured_from_fresh_thread(cuda, medium_model):
     assert "err" not in out, out.get("err")
     assert np.array_equal(out["img"], ref, equal_nan=True)
     assert ref.max() > 0
+
+
+def test_camera_states_precomputed_equal_inline(cuda, medium_model):
+    """A mixed launch larger than one wave of phase A (4 blocks per SM)
+    takes its camera states from a separate FP64 kernel when the workspace
+    has room for them (mk_render_workspace_bytes); with a workspace of the
+    base size phase A computes them itself.  The images are bit-identical."""
+    import torch
+
+    from mahakala_gb300 import _lib
+    from mahakala_gb300._device import ptr, stream_ptr
+    from mahakala_gb300.images import PreparedRender, RenderRequest
+    sms = _lib.load().mk_device_sm_count()
+    res = int(np.ceil(np.sqrt(sms * 4 * 128 + 1)))  # just over one wave
+    kw = dict(camera_inclination=17.0, resolution=res, fov=50.0, max_nsteps=4096)
+    full = PreparedRender([RenderRequest(medium_model, **kw)], precision="mixed")
+    base = 256 + 320 * full.total_rays
+    assert full.ws.numel() * 8 >= base + 64 * full.total_rays
+    full.launch()
+    small = PreparedRender([RenderRequest(medium_model, **kw)], precision="mixed")
+    _lib.call("mk_render", ptr(small.reqs_dev), 1, small.total_rays, ptr(small.snaps_dev), small.nsnap,
+              small.precision, ptr(small.ws), base, stream_ptr(None))
+    torch.cuda.synchronize()
+    a, b = full.images[0].cpu().numpy(), small.images[0].cpu().numpy()
+    assert a.max() > 0
+    assert np.array_equal(a, b, equal_nan=True)
