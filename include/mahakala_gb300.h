@@ -262,9 +262,14 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
 /* ------------------------------------------------------- fused render */
 /* Scratch bytes mk_render needs in workspace_dev for total_rays rays at
    the given precision: a 256-byte header of counters (MK_FP64), plus two
-   ray queues of total_rays records each for the hand-offs between the
-   FP32 and FP64 phases (MK_MIXED).  The caller allocates it (16-byte
-   aligned) and may reuse it for calls that do not overlap on the device.
+   ray queues of total_rays 160-byte records each for the hand-offs between
+   the phases (mixed forms), plus -- when total_rays is more than one wave
+   of the FP32 phase on the current device (4 blocks of 128 threads per SM)
+   -- 64 bytes a ray for camera states computed ahead of it.  A workspace of
+   at least the size without that last part also renders (the FP32 phase
+   then computes the camera states itself, more slowly).  The caller
+   allocates it (16-byte aligned) and may reuse it for calls that do not
+   overlap on the device.
    After a launch the header holds, as uint64 at these word offsets, the
    launch's totals: MK_WS_STEPS accepted RK4 steps, MK_WS_SAMPLES
    in-snapshot samples, MK_WS_MAX_TAU the bits of a double, the largest
