@@ -55,8 +55,15 @@ def test_version_and_workspace(lib):
     assert lib.mk_abi_version() == 1
     assert b"sm_103a" in lib.mk_version()
     assert lib.mk_render_workspace_bytes(100, 0) == 256
-    assert lib.mk_render_workspace_bytes(100, 1) > 256 + 2 * 100 * 100
     assert lib.mk_snapshot_bytes(8, 8) == 8 * 10 ** 3 * 32 + 8 * 32
+    # mixed forms: two queues of 160-byte records, plus 64 bytes a ray of
+    # camera states once the launch exceeds one wave of 4 blocks x 128
+    # threads per SM (the SM count the library reports; 1 without a GPU)
+    wave = lib.mk_device_sm_count() * 4 * 128
+    for n in (100, wave, wave + 1, 4 * wave):
+        for prec in (_lib.MK_MIXED, _lib.MK_MIXED_STRICT, _lib.MK_MIXED_DF):
+            assert lib.mk_render_workspace_bytes(n, prec) == 256 + 320 * n + (64 * n if n > wave else 0)
+        assert lib.mk_render_workspace_bytes(n, _lib.MK_FP64) == 256
 
 
 def test_argument_errors_without_gpu(lib):
