@@ -59,6 +59,7 @@ def test_version_and_workspace(lib):
     # mixed forms: two queues of 160-byte records, plus 64 bytes a ray of
     # camera states once the launch exceeds one wave of 4 blocks x 128
     # threads per SM (the SM count the library reports; 1 without a GPU)
+    from mahakala_gb300 import _lib
     wave = lib.mk_device_sm_count() * 4 * 128
     for n in (100, wave, wave + 1, 4 * wave):
         for prec in (_lib.MK_MIXED, _lib.MK_MIXED_STRICT, _lib.MK_MIXED_DF):
