@@ -19,7 +19,7 @@ FP64 render keeps the reference's explicit Euler transfer stable (see
 MASS_SCALE_256).
 """
 
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 from .constants import PARSEC, Msun
 

@@ -8,7 +8,6 @@ sm_103a kernel (``mk_render``); no trajectory is materialised, so
 is accepted for compatibility only.
 """
 
-import ctypes
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -17,7 +16,7 @@ import torch
 from . import _lib
 from ._device import device, ptr, stream_ptr
 from .constants import JY, Msun
-from .geodesics import camera_pixels, make_camera, step_policy
+from .geodesics import make_camera, step_policy
 
 __all__ = ["make_image", "RenderRequest", "PreparedRender", "render_requests", "image_flux_jy", "step_diagnostics"]
 

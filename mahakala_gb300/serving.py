@@ -26,7 +26,7 @@ import collections
 import ctypes
 import itertools
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 

@@ -4,7 +4,6 @@ synchrotron, transfer.  Every call goes through libmahakala_gb300.so."""
 
 import numpy as np
 import pytest
-import torch
 
 from conftest import golden, rel_err
 
