@@ -109,3 +109,42 @@ def test_render_rejects_missing_fluid_gamma(cuda, tiny_arrays):
     model = _model(tiny_arrays, fluid_gamma=None)
     with pytest.raises(TypeError):
         make_image(model, resolution=4)
+
+
+@pytest.mark.parametrize("res", [1, 2, 3])
+def test_tiny_images_every_form(cuda, orc, tiny_arrays, res):
+    """1x1, 2x2 and 3x3 images -- a single ray and warps with 1, 4 or 9 live
+    lanes of 32: the FP64 form within the parity bar of the oracle, the
+    mixed forms within their bars of the FP64 image."""
+    from mahakala_gb300 import metrics
+    from mahakala_gb300.grmhd.athenak import AthenakFluidModel
+    from mahakala_gb300.images import make_image
+    model = AthenakFluidModel(tiny_arrays, tiny_arrays.bhspin, fluid_gamma=13. / 9)
+    kw = dict(camera_inclination=60, mass_scale=1e27, r_high=3, fov=30, resolution=res, max_nsteps=2000)
+    img = make_image(model, **kw)
+    o = orc.make_image(orc.OracleSnapshot(tiny_arrays), **kw)
+    assert img.shape == o.shape == (res, res)
+    assert np.max(rel_err(img, o, floor=1e-4 * max(np.abs(o).max(), 1e-300))) < 1e-8
+    for form in ("mixed", "mixed_strict", "mixed_df"):
+        mixed = make_image(model, precision=form, **kw)
+        assert np.all(np.isfinite(mixed))
+        assert metrics.max_pixel_rel_err(mixed, img) <= 1e-2, form
+        assert metrics.flux_rel_err(mixed, img) <= 1e-3, form
+
+
+def test_render_of_zero_rays_is_a_no_op(cuda, tiny_arrays):
+    """total_rays = 0: mk_render returns MK_OK and writes no image."""
+    import torch
+
+    from mahakala_gb300 import _lib
+    from mahakala_gb300._device import ptr, stream_ptr
+    from mahakala_gb300.grmhd.athenak import AthenakFluidModel
+    from mahakala_gb300.images import PreparedRender, RenderRequest
+    model = AthenakFluidModel(tiny_arrays, tiny_arrays.bhspin, fluid_gamma=13. / 9)
+    for form in ("fp64", "mixed"):
+        prep = PreparedRender([RenderRequest(model, resolution=4, fov=30)], precision=form)
+        prep.images[0].fill_(-7.0)
+        _lib.call("mk_render", ptr(prep.reqs_dev), 1, 0, ptr(prep.snaps_dev), prep.nsnap, prep.precision,
+                  ptr(prep.ws), prep.ws.numel() * 8, stream_ptr(None))
+        torch.cuda.synchronize()
+        assert bool((prep.images[0] == -7.0).all()), form
