@@ -11,9 +11,15 @@ snapshot at 256x256 pixels (a=0.94, 17 deg, 230 GHz, <= 8192 steps), timed
 in every form -- plain FP64 and the mixed FP32/FP64 forms (mixed,
 mixed_strict, mixed_df) -- with each mixed form's flux and per-pixel error
 against the FP64 image of the same run.  The headline value is the mixed
-form's rays/s.  ``--workload stress1024``: the 512^3-cell snapshot at
-1024x1024, three frequencies in one pass, <= 16384 steps.  Printed on rank
-0 as one JSON line.
+form's rays/s.  The default run also prints: the FP64 image checked
+against the oracle's render of the same rays (``fp64_vs_oracle``) and each
+mixed form's error against it (``mixed_vs_oracle``), the FP64 form end to
+end (``e2e_fp64``, ``fp64_vs_reference``), the standalone sampling stage
+(``sampling_stage``), the served Poisson stream (``serving``), the
+1024x1024 stress render in both forms (``stress1024``) and the 27-image
+512x512 mixed-precision sweep (``sweep512``).  ``--workload stress1024``:
+the 512^3-cell snapshot at 1024x1024, three frequencies in one pass,
+<= 16384 steps, as the headline.  Printed on rank 0 as one JSON line.
 
 ``--impl reference`` times the reference algorithm on the host cores
 instead: the C restatement of Mahakala's make_image (oracle/, FP64, all
@@ -73,8 +79,13 @@ def parse():
     p.add_argument("--serving", type=int, default=60,
                    help="requests in the served Poisson stream (0 = skip the serving measurement)")
     p.add_argument("--sampling-rays", type=int, default=-1,
-                   help="rays per side of the standalone sampling-stage measurement (0 = skip; default 128 for "
-                        "stress1024, 0 otherwise)")
+                   help="rays per side of the standalone sampling-stage measurement (0 = skip; default 128)")
+    p.add_argument("--stress", type=int, default=1,
+                   help="1: the default run also times the 1024x1024 three-frequency stress render in the mixed "
+                        "form and in FP64 (the 'stress1024' key); 0: skip it")
+    p.add_argument("--sweep", type=int, default=1,
+                   help="1: the default run also renders the 27-image 512x512 mixed-precision sweep (spin x "
+                        "inclination x R_high, each image in FP64 and mixed; the 'sweep512' key); 0: skip it")
     p.add_argument("--quick", action="store_true",
                    help="device timing only: skip the FMA probes, the end-to-end pass and the CPU baseline")
     return p.parse_args()
@@ -143,25 +154,60 @@ def clocks_summary(proc, f, path, gpu_index):
             "samples": len(sm)}
 
 
-def measure_fma_peak(torch, precision):
-    """FMA probe: achieved FLOP/s of 8 independent FMA chains per thread."""
+def measure_fma_peak(torch, kind):
+    """FMA probe: achieved FLOP/s of 8 independent FMA chains per thread
+    (kind MK_FP64 or MK_MIXED = FP32), or 8 chains of paired FP32 FMAs
+    (MK_PROBE_FFMA2, 16 FMAs per iteration)."""
     from mahakala_gb300 import _lib
     lib = _lib.load()
     sms = lib.mk_device_sm_count()
     blocks, threads = sms * 8, 256
-    iters = 4096 if precision == _lib.MK_FP64 else 65536
+    iters = 4096 if kind == _lib.MK_FP64 else 65536
+    fma_per_iter = 16 if kind == _lib.MK_PROBE_FFMA2 else 8
     out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
     s = torch.cuda.current_stream()
     best = 0.0
     for _ in range(3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
-        _lib.call("mk_probe_fma", precision, blocks, threads, iters, out.data_ptr(), s.cuda_stream)
+        _lib.call("mk_probe_fma", kind, blocks, threads, iters, out.data_ptr(), s.cuda_stream)
         e1.record(s)
         e1.synchronize()
         t = e0.elapsed_time(e1) * 1e-3
-        best = max(best, 2.0 * 8 * iters * blocks * threads / t)
+        best = max(best, 2.0 * fma_per_iter * iters * blocks * threads / t)
     return best
+
+
+def sm_max_mhz(gpu_index):
+    """The GPU's maximum SM clock (MHz) from nvidia-smi, else the measured-peak
+    file's figure, else None."""
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits",
+                              "-i", str(gpu_index)], capture_output=True, text=True, timeout=20).stdout
+        return float(out.strip().splitlines()[0])
+    except (OSError, ValueError, IndexError, subprocess.SubprocessError):
+        pass
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["sm_max_mhz"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def probe_peaks(torch, gpu_index):
+    """ALU peaks of this GPU: the FP64 FMA probe, the FP32 FMA probe, the
+    paired-FP32 FMA probe and the FP32 issue limit SMs x 128 lanes x 2 FLOP
+    x the maximum SM clock.  The FP32 roofline peak is the largest of the
+    last three (a kernel cannot beat any of them)."""
+    from mahakala_gb300 import _lib
+    sms = _lib.load().mk_device_sm_count()
+    mhz = sm_max_mhz(gpu_index)
+    p64 = measure_fma_peak(torch, _lib.MK_FP64)
+    p32 = measure_fma_peak(torch, _lib.MK_MIXED)
+    p2 = measure_fma_peak(torch, _lib.MK_PROBE_FFMA2)
+    theo = sms * 128 * 2 * mhz * 1e6 if mhz else 0.0
+    return {"fp64": p64, "fp32": max(p32, p2, theo), "fp32_probe": p32, "ffma2_probe": p2,
+            "fp32_theoretical": theo, "sms": sms, "sm_max_mhz": mhz}
 
 
 def cpu_sample_pixels(res, want):
@@ -172,20 +218,53 @@ def cpu_sample_pixels(res, want):
 
 def cpu_baseline(spec, arrays, rays_wanted, threads):
     """The oracle (C restatement of the reference, FP64) on a strided pixel
-    subset of the same image; returns (rays/s, sample description)."""
+    subset of the same image; returns (rays/s, sample description, oracle
+    run).  The oracle run -- its image, steps and pixel indices, plus an
+    untimed second run with each initial wavevector perturbed by 1e-12 that
+    tells well-conditioned rays from grazing ones -- is the checker the
+    FP64 GPU image is compared against."""
     import oracle
     os.environ["OMP_NUM_THREADS"] = str(threads)
     snap = oracle.OracleSnapshot(arrays)
     pix, stride = cpu_sample_pixels(spec.resolution, rays_wanted)
     s0 = oracle.initialize_geodesics_at_camera(spec.bhspin, spec.inclination, spec.camera_distance,
                                                -spec.half_fov, spec.half_fov, spec.resolution)[pix]
+    args = (spec.mass_scale, spec.M_bh, spec.r_high, list(spec.freqs), spec.max_nsteps, spec.r_low)
     t0 = time.perf_counter()
-    oracle.render_rays(snap, s0, spec.mass_scale, spec.M_bh, spec.r_high, list(spec.freqs), spec.max_nsteps,
-                       spec.r_low)
+    img, steps = oracle.render_rays(snap, s0, *args)
     dt = time.perf_counter() - t0
+    pimg, psteps = oracle.render_rays(snap, oracle.perturbed(s0), *args)
     what = "the whole image" if stride == 1 else f"every {stride}th pixel in x and y of the same image"
+    run = dict(pix=pix, img=img, steps=steps, pert_img=pimg, pert_steps=psteps)
     return len(pix) / dt, (f"{len(pix)} rays ({what}), full FP64 physics, {threads} OpenMP threads; "
-                           f"{dt:.1f} s")
+                           f"{dt:.1f} s"), run
+
+
+def oracle_checks(res, run, nnu):
+    """fp64_vs_oracle: the FP64 GPU image at the oracle's pixels against the
+    oracle's image (oracle.image_parity: equal steps, pixels and flux within
+    1e-8 on the well-conditioned rays); mixed_vs_oracle: each mixed form's
+    flux and max pixel error against the oracle's image directly (floor
+    1e-4 of the maximum), beside its bars (1e-3, 1e-2)."""
+    import oracle
+    from mahakala_gb300 import metrics
+    pix = run["pix"]
+    out = {}
+    if "fp64" in res:
+        r = res["fp64"]
+        img = r["image"].reshape(nnu, -1)[:, pix].cpu().numpy()
+        steps = r["req"].out["nsteps"].reshape(-1)[pix].cpu().numpy()
+        out["fp64_vs_oracle"] = oracle.image_parity(img, steps, run["img"], run["steps"], run["pert_img"],
+                                                    run["pert_steps"])
+    for form in ("mixed", "mixed_strict", "mixed_df"):
+        if form in res:
+            img = res[form]["image"].reshape(nnu, -1)[:, pix].cpu().numpy()
+            out[form + "_vs_oracle"] = {
+                "flux_rel_err": max(metrics.flux_rel_err(img[c], run["img"][c]) for c in range(nnu)),
+                "max_pixel_rel_err": max(metrics.max_pixel_rel_err(img[c], run["img"][c]) for c in range(nnu)),
+                "rays": int(len(pix)), "bars": {"flux": 1e-3, "pixel": 1e-2},
+                "pixel_floor": "max(|I_oracle|, 1e-4 max I_oracle)"}
+    return out
 
 
 def run_reference(args):
@@ -266,7 +345,7 @@ def run_reference_vacuum(args):
     print(json.dumps(line), flush=True)
 
 
-def time_render(torch, prep, stream, steps, warmup, flush, barrier):
+def time_render(torch, prep, stream, steps, warmup, flush, barrier, min_warmup=3):
     """W warm-up launches, then K launches each timed by CUDA events on the
     launching stream with an L2 flush (untimed) before each.  The library
     also records events on that stream around each of the render's kernels
@@ -274,7 +353,7 @@ def time_render(torch, prep, stream, steps, warmup, flush, barrier):
     (s) and the per-kernel times (s) of every timed step."""
     import ctypes
     from mahakala_gb300 import _lib
-    for _ in range(max(warmup, 3)):
+    for _ in range(max(warmup, min_warmup)):
         prep.launch(stream)
     torch.cuda.synchronize()
     barrier()
@@ -410,6 +489,52 @@ def sampling_stage(torch, model, spec, flush, stream, fp64_peak, rays_per_side=1
                     "FLOP per point from ncu's FP64 instruction counters on the same case"}
 
 
+def stress_record(torch, stream, flush, peaks):
+    """The 1024x1024 stress render (512^3-cell snapshot, a=0.94, 60 deg,
+    86/230/345 GHz in one ray pass, <= 16384 steps) in the mixed form and in
+    FP64, each CUDA-event timed with per-kernel times, with each mixed
+    channel's flux and pixel error against the FP64 image.  Mixed: 3
+    warm-up and 3 timed renders; FP64 (1.3 s a render): 1 and 1."""
+    from mahakala_gb300 import configs, metrics
+    from mahakala_gb300.grmhd.athenak import AthenakFluidModel
+    from mahakala_gb300.images import PreparedRender
+    spec, desc = workload("stress1024", 0, "mixed and fp64")
+    t0 = time.perf_counter()
+    model = AthenakFluidModel(spec.snapshot.build(), spec.snapshot.bhspin, fluid_gamma=spec.snapshot.fluid_gamma)
+    t_build = time.perf_counter() - t0
+    rays, nnu = spec.resolution ** 2, len(spec.freqs)
+    per_sample = FLOP_PER_SAMPLE + FLOP_PER_EXTRA_NU * (nnu - 1)
+    out = {"workload": desc, "snapshot_build_s": t_build, "mass_scale": spec.mass_scale}
+    imgs = {}
+    for form, reps, warm in (("mixed", 3, 3), ("fp64", 1, 1)):
+        prep = PreparedRender([spec.request(model)], precision=form, with_steps=True)
+        times, phases = time_render(torch, prep, stream, reps, warm, flush, torch.cuda.synchronize,
+                                    min_warmup=warm)
+        t = statistics.mean(times)
+        steps, samples = prep.work_totals()
+        flops = steps * FLOP_PER_STEP + samples * per_sample
+        pk = peaks["fp64"] if form == "fp64" else peaks["fp32"]
+        out[form] = {"rays_per_s": rays / t, "ms": 1e3 * t, "images_per_s": nnu / t,
+                     "phase_ms": [1e3 * statistics.mean(p[i] for p in phases) for i in range(len(phases[0]))],
+                     "accepted_steps": steps, "samples": samples, "ray_steps_per_s": steps / t,
+                     "achieved_tflops": flops / t / 1e12, "peak_tflops": pk / 1e12, "frac": flops / t / pk,
+                     "max_step_optical_depth": prep.max_step_optical_depth(), "timed_renders": reps}
+        imgs[form] = (prep.images[0].clone(), prep.requests[0].out["status"].clone())
+        del prep
+    errs = [metrics.compare(imgs["mixed"][0][c], imgs["fp64"][0][c], imgs["mixed"][1], imgs["fp64"][1], spec.fov)
+            for c in range(nnu)]
+    out["mixed_vs_fp64"] = {"speedup": out["fp64"]["ms"] / out["mixed"]["ms"],
+                            "channels_ghz": [f / 1e9 for f in spec.freqs],
+                            "flux_rel_err": [e["flux_rel_err"] for e in errs],
+                            "max_pixel_rel_err": [e["max_pixel_rel_err"] for e in errs],
+                            "shadow_diameter": errs[0]["shadow_diameter"],
+                            "shadow_diameter_fp64": errs[0]["shadow_diameter_fp64"],
+                            "pixel_floor": "max(|I_fp64|, 1e-4 max I_fp64)"}
+    del imgs, model
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_vacuum(args):
     """Config-1 vacuum trace: 128x128 rays, a=0.94, 60 deg, +-10 M, <= 4096
     steps, end states only (no trajectory rows), under the reference step
@@ -525,8 +650,9 @@ def main():
     model = AthenakFluidModel(arrays, spec.snapshot.bhspin, fluid_gamma=spec.snapshot.fluid_gamma)
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    peak64 = measure_fma_peak(torch, _lib.MK_FP64) if not args.quick else float("nan")
-    peak32 = measure_fma_peak(torch, _lib.MK_MIXED) if not args.quick else float("nan")
+    peaks = probe_peaks(torch, local) if not args.quick else None
+    peak64 = peaks["fp64"] if peaks else float("nan")
+    peak32 = peaks["fp32"] if peaks else float("nan")
 
     def barrier():
         if world > 1:
@@ -560,7 +686,7 @@ def main():
     clocks = clocks_summary(proc, fh, cpath, local) if rank == 0 else None
 
     sampling = None
-    srays = args.sampling_rays if args.sampling_rays >= 0 else (128 if args.workload == "stress1024" else 0)
+    srays = args.sampling_rays if args.sampling_rays >= 0 else 128
     if srays:
         sampling = sampling_stage(torch, model, spec, flush, stream, peak64 if not args.quick else float("nan"),
                                   rays_per_side=srays)
@@ -569,6 +695,20 @@ def main():
     if args.serving and not args.quick and args.workload == "render256" and rank == 0:
         # one GPU's serving stream (the other replicas would repeat it)
         serving = run_serving(torch, model, args.serving, [f for f in ("mixed", "fp64") if f in forms])
+
+    sweep = None
+    if args.sweep and not args.quick and args.workload == "render256" and not args.resolution and rank == 0:
+        from mahakala_gb300 import sweep as sweepmod
+        t0 = time.perf_counter()
+        rep = sweepmod.run(512, "mixed", model=model)
+        keep = ("spin", "inclination", "r_high", "fp64_ms", "mixed_ms", "speedup", "max_pixel_rel_err",
+                "flux_rel_err", "shadow_diameter_rel_err", "max_step_optical_depth")
+        sweep = dict(rep, rows=[{k: r[k] for k in keep} for r in rep["rows"]], wall_s=time.perf_counter() - t0,
+                     timing="one warm launch per form and image, CUDA events")
+
+    stress = None
+    if args.stress and not args.quick and args.workload == "render256" and not args.resolution and rank == 0:
+        stress = stress_record(torch, stream, flush, peaks)
 
     # end to end through the public API: host request in, NumPy image out
     # (W untimed calls first, like the device timing)
@@ -583,10 +723,23 @@ def main():
         if k >= max(args.warmup, 3):
             e2e_times.append(time.perf_counter() - t0)
     e2e_t = statistics.mean(e2e_times) if e2e_times else float("nan")
+    # the FP64 form end to end too (like for like against the FP64 CPU path)
+    e2e64_times = []
+    if head != "fp64" and "fp64" in forms:
+        for k in range(0 if args.quick else max(args.warmup, 3) + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            make_image(model, camera_inclination=spec.inclination, camera_distance=spec.camera_distance,
+                       mass_scale=spec.mass_scale, M_bh=spec.M_bh, r_high=spec.r_high,
+                       observing_frequency=list(spec.freqs) if nnu > 1 else spec.freqs[0], fov=spec.fov,
+                       resolution=spec.resolution, max_nsteps=spec.max_nsteps, precision="fp64")
+            if k >= max(args.warmup, 3):
+                e2e64_times.append(time.perf_counter() - t0)
+    e2e64_t = statistics.mean(e2e64_times) if e2e64_times else float("nan")
     if world > 1 and e2e_times:  # the slowest replica sets the job's rate
-        t = torch.tensor([e2e_t], device="cuda")
+        t = torch.tensor([e2e_t, e2e64_t], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(t.item())
+        e2e_t, e2e64_t = float(t[0].item()), float(t[1].item())
     L_unit = model.get_units(spec.M_bh, spec.mass_scale)["L_unit"]
 
     def roofline(form):
@@ -594,8 +747,9 @@ def main():
         the library records around each kernel of every timed step."""
         r = res[form]
         per_sample = FLOP_PER_SAMPLE + FLOP_PER_EXTRA_NU * (nnu - 1)
-        src = ("FMA probe measured in this run (mk_probe_fma); the measured-peak file holds no FP64/FP32 "
-               "ALU figure")
+        src = ("FP64: the FMA probe measured in this run (mk_probe_fma); FP32: the largest of the FP32 FMA "
+               "probe, the paired-FP32 FMA probe and the issue limit SMs x 128 x 2 FLOP x the maximum SM clock; "
+               "the measured-peak file holds no FP64/FP32 ALU figure")
         if form == "fp64":
             kernels = [("render_fp64_kernel", "fp64", r["steps"] * FLOP_PER_STEP + r["samples"] * per_sample,
                         r["t_phase"][0], peak64, None)]
@@ -624,7 +778,9 @@ def main():
         out = {"bound": top["bound"], "achieved": top["achieved"], "peak": top["peak"], "unit": "TFLOP/s",
                "frac": top["frac"], "traffic": top["traffic"], "kernel": top["kernel"], "flop_per_launch": top["flop"],
                "kernel_ms": top["ms"], "peak_source": src, "kernels": table,
-               "peak_fp32_tflops": peak32 / 1e12, "peak_fp64_tflops": peak64 / 1e12}
+               "peak_fp32_tflops": peak32 / 1e12, "peak_fp64_tflops": peak64 / 1e12,
+               "peaks_tflops": {k: (v / 1e12 if k.startswith(("fp", "ffma")) else v)
+                                for k, v in (peaks or {}).items()}}
         if top["traffic"] is not None:
             out["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
                                      "kernel on this workload (bytes per launch); the kernels are ALU- and "
@@ -659,12 +815,13 @@ def main():
         return
     threads = os.cpu_count() or 1
     if args.quick:
-        cpu_val, cpu_sample = None, "skipped (--quick)"
+        cpu_val, cpu_sample, cpu_run = None, "skipped (--quick)", None
     else:
         # the whole image up to 262,144 rays (a strided quarter of the 1024x1024
         # workload): ~3 s on 16 cores at 256x256, ~16 s at 1024x1024
-        cpu_val, cpu_sample = cpu_baseline(spec, arrays, args.cpu_sample_rays or min(spec.resolution ** 2, 1 << 18),
-                                           threads)
+        cpu_val, cpu_sample, cpu_run = cpu_baseline(spec, arrays,
+                                                    args.cpu_sample_rays or min(spec.resolution ** 2, 1 << 18),
+                                                    threads)
     line = {
         "metric": "rays/s", "value": world * rays / t_head, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_head, "higher_is_better": True, "scaling": "weak",
@@ -691,6 +848,8 @@ def main():
                                    "shadow_diameter": errs[0]["shadow_diameter"],
                                    "shadow_diameter_fp64": errs[0]["shadow_diameter_fp64"],
                                    "pixel_floor": "max(|I_fp64|, 1e-4 max I_fp64)"}
+    if cpu_run is not None:
+        line.update(oracle_checks(res, cpu_run, nnu))
     line.update({
         "roofline": roofline(head),
         "cpu_baseline": {"value": cpu_val, "unit": "rays/s", "cores": threads, "kind": "port",
@@ -698,8 +857,19 @@ def main():
         "e2e": {"value": world * rays / e2e_t, "unit": "rays/s", "h2d_bytes_per_step": len(res[head]["prep"].table_bytes),
                 "d2h_bytes_per_step": int(rays * nnu * 8),
                 "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
+        "e2e_fp64": ({"value": world * rays / e2e64_t, "unit": "rays/s",
+                      "h2d_bytes_per_step": len(res["fp64"]["prep"].table_bytes),
+                      "d2h_bytes_per_step": int(rays * nnu * 8),
+                      "api": "mahakala_gb300.images.make_image(precision='fp64') (host request -> NumPy image)"}
+                     if e2e64_times else None),
+        "fp64_vs_reference": ({"e2e_ratio": (world * rays / e2e64_t) / cpu_val,
+                               "device_ratio": (world * rays / res["fp64"]["t_step"]) / cpu_val,
+                               "note": "FP64 GPU form over the FP64 CPU path (cpu_baseline), like for like"}
+                              if e2e64_times and cpu_val else None),
         "serving": serving,
         "sampling_stage": sampling,
+        "stress1024": stress,
+        "sweep512": sweep,
         # per render: FP64 one kernel; mixed forms A, B, C, plus the camera-state
         # kernel when the launch exceeds one wave of phase A at 4 blocks per SM
         "gpu_launches": args.steps * (1 if head == "fp64" else

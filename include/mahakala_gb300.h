@@ -312,7 +312,9 @@ size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision);
    camera -> geodesics -> sampling -> electrons -> synchrotron -> sigma cut ->
    transfer, fused per ray; no trajectory is stored.  reqs_dev (nreq)
    device array with ray_offset the exclusive prefix sum of the requests'
-   pixel counts; total_rays the sum.  snaps_dev (nsnap) device array of
+   pixel counts; total_rays the sum (ray indices that fall outside their
+   request's pixels -- a total_rays above the sum -- are skipped, nothing
+   written).  snaps_dev (nsnap) device array of
    views.  precision: mk_precision.  Request images receive the specific
    intensity the reference's solve_specific_intensity returns. */
 int mk_render(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
@@ -344,10 +346,11 @@ int mk_render_job(const mk_job *job_dev, const mk_request *reqs_dev, const mk_sn
    MK_NOALLOC_WORKSPACE_BYTES that every GPU loading the library holds until
    exit.  The caller still passes requests, snapshots and images.  Limit:
    any ray count in MK_FP64; at most MK_NOALLOC_MAX_MIXED_RAYS rays per call
-   in the mixed forms (larger jobs return MK_ERR_LIMIT).  The first call on
-   a device looks the array up (cudaGetSymbolAddress) and should come before
-   any stream capture.  All calls share the array: calls that overlap on the
-   GPU race. */
+   in the mixed forms (larger jobs return MK_ERR_LIMIT), on every GPU.  The
+   first call on a device looks the array up (cudaGetSymbolAddress) and
+   should come before any stream capture; a later call that finds another
+   CUDA context current on that device (after a reset) looks it up again.
+   All calls share the array: calls that overlap on the GPU race. */
 #define MK_NOALLOC_WORKSPACE_BYTES (16u << 20)
 #define MK_NOALLOC_MAX_MIXED_RAYS ((MK_NOALLOC_WORKSPACE_BYTES - 256u) / 320u)
 int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
@@ -376,10 +379,12 @@ int mk_render_phase_ms(float *ms_out, int32_t *nphases);
 
 /* ------------------------------------------------------------ probes */
 /* FMA throughput probe (no reference counterpart): blocks x threads
-   threads each run iters x 8 dependent-chain FMAs in FP64
-   (precision MK_FP64) or FP32 (MK_MIXED); time it with events to get the
-   ALU peak a roofline is reported against.  out_dev: blocks*threads
-   elements of that type. */
+   threads each run iters x 8 independent-chain FMAs in FP64 (precision
+   MK_FP64), FP32 (MK_MIXED), or iters x 8 paired FP32 FMAs, 16 FMAs
+   (MK_PROBE_FFMA2); time it with events to get the ALU peak a roofline is
+   reported against.  out_dev: blocks*threads elements of that type
+   (float for MK_PROBE_FFMA2).  iters <= 2^30. */
+#define MK_PROBE_FFMA2 100
 int mk_probe_fma(int32_t precision, int32_t blocks, int32_t threads, int64_t iters, void *out_dev,
                  void *stream);
 

@@ -24,6 +24,7 @@ MK_FP64, MK_MIXED, MK_MIXED_DF, MK_MIXED_STRICT = 0, 1, 2, 3
 MK_POLICY_REFERENCE, MK_POLICY_FIXED = 0, 1
 MK_CAMERA_GRID, MK_CAMERA_EQUATOR = 0, 1
 MK_MAX_NU = 4
+MK_PROBE_FFMA2 = 100
 NOALLOC_WORKSPACE_BYTES = 16 << 20
 NOALLOC_MAX_MIXED_RAYS = (NOALLOC_WORKSPACE_BYTES - 256) // 320
 MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_FP32_QUEUE, MK_WS_STEPS_FP64 = 1, 2, 3, 4, 6, 8

@@ -12,6 +12,10 @@ namespace mk {
 
 void set_error(const char *fmt, ...);
 int device_sm_count();
+// scratch bytes mk_render cannot do without: the counter header and, in the
+// mixed forms, the two ray queues (mk_render_workspace_bytes may add an
+// optional camera-state region on top)
+size_t render_ws_base(int64_t rays, int32_t precision);
 
 #define MK_REQUIRE(cond, code, ...)        \
     do {                                   \

@@ -180,6 +180,16 @@ __device__ __forceinline__ int64_t request_pixels(const mk_camera &c) {
     return c.kind == MK_CAMERA_EQUATOR ? (int64_t)c.pixels : (int64_t)c.pixels * c.pixels;
 }
 
+// false for a ray index outside its request's pixels, which happens only
+// when total_rays exceeds the sum of the requests' pixel counts (a caller
+// error the host cannot see: the table is on the device); such a ray is
+// skipped, so no image is written out of bounds
+__device__ __forceinline__ bool ray_in_request(const mk_request *__restrict__ reqs, int nreq, long long ray) {
+    const int rq = find_request(reqs, nreq, ray);
+    const long long pix = ray - reqs[rq].ray_offset;
+    return pix >= 0 && pix < request_pixels(reqs[rq].camera);
+}
+
 // warp-aggregated work fetch: returns this lane's item index, -1 when the
 // lane asked and the work is exhausted, -2 when the lane did not ask
 __device__ __forceinline__ long long fetch(bool want, unsigned long long *counter, long long total) {
@@ -477,7 +487,7 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
         const long long idx = fetch(lane_works && !active && !exhausted, counter, total);
         if (idx == -1) exhausted = true;
         if (!lane_works) exhausted = true;
-        if (idx >= 0) {
+        if (idx >= 0 && (SRC != SRC_CAMERA || ray_in_request(reqs, nreq, idx))) {
             if (SRC == SRC_CAMERA) {
                 ray = idx;
                 rq = find_request(reqs, nreq, ray);
@@ -912,6 +922,7 @@ camera_states_kernel(const mk_request *__restrict__ reqs, int nreq, long long to
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
          p += (long long)gridDim.x * blockDim.x) {
         const int rq = find_request(reqs, nreq, p);
+        if (!ray_in_request(reqs, nreq, p)) continue;
         double s[8];
         camera_ray(reqs[rq].camera, p - reqs[rq].ray_offset, s);
 #pragma unroll
@@ -953,7 +964,7 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
     for (;;) {
         const long long idx = fetch(!active && !exhausted, counter, total);
         if (idx == -1) exhausted = true;
-        if (idx >= 0) {
+        if (idx >= 0 && (SRC != SRC_CAMERA || ray_in_request(reqs, nreq, idx))) {
             double s64[8];
             if (SRC == SRC_CAMERA) {
                 ray = idx;
@@ -1146,6 +1157,7 @@ static bool mixed_form(int32_t precision) {
 static size_t ws_base(int64_t rays, int32_t precision) {
     return mixed_form(precision) ? WS_HEADER + 2 * (size_t)rays * sizeof(RayRecord) : WS_HEADER;
 }
+size_t render_ws_base(int64_t rays, int32_t precision) { return ws_base(rays, precision); }
 static bool camera_precompute(int64_t rays, int32_t precision) {
     return mixed_form(precision) && rays > (int64_t)device_sm_count() * 4 * RENDER_THREADS;
 }

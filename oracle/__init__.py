@@ -485,3 +485,43 @@ def _with_spin(snapshot, a):
     s = copy.copy(snapshot)
     s.bhspin = float(a)
     return s
+
+
+def image_parity(img, steps, ref_img, ref_steps, pert_img, pert_steps, floor_frac=1e-4, ill_tol=1e-10,
+                 bar=1e-8):
+    """Checker of an FP64 image against the oracle's render of the same rays.
+
+    img, ref_img, pert_img: (nnu, n) intensities of the same n rays -- the
+    image under test, the oracle, and the oracle with each ray's initial
+    wavevector perturbed by 1e-12 (``perturbed``); steps, ref_steps,
+    pert_steps: (n,) accepted steps per ray.  A ray is ill-conditioned when
+    the perturbed oracle run changes its step count or moves any channel by
+    more than ``ill_tol`` relative (floor ``floor_frac`` of the channel's
+    maximum): two FP64 evaluation orders then legitimately differ by more
+    than rounding.  On the conditioned rays the steps must be equal, every
+    pixel within ``bar`` relative and the summed flux within ``bar``.
+    Returns a dict of the counts and errors and ``ok``."""
+    img, ref, pert = (np.atleast_2d(np.asarray(x, dtype=np.float64)) for x in (img, ref_img, pert_img))
+    steps, ref_steps, pert_steps = (np.asarray(x).reshape(-1) for x in (steps, ref_steps, pert_steps))
+    floor = floor_frac * np.abs(ref).max(axis=1, keepdims=True)
+
+    def rel(a, b):
+        den = np.maximum(np.abs(b), floor)
+        with np.errstate(all="ignore"):
+            e = np.abs(a - b) / np.where(den > 0, den, 1.0)
+        return np.where((a == b) | (np.isnan(a) & np.isnan(b)), 0.0, e)
+
+    ill = (pert_steps != ref_steps) | (rel(pert, ref) > ill_tol).any(axis=0)
+    ok_rays = ~ill
+    n_ok = int(ok_rays.sum())
+    steps_equal = bool(np.array_equal(steps[ok_rays], ref_steps[ok_rays]))
+    err = rel(img, ref)
+    max_pix = float(err[:, ok_rays].max()) if n_ok else 0.0
+    fl, fl_ref = img[:, ok_rays].sum(axis=1), ref[:, ok_rays].sum(axis=1)
+    with np.errstate(all="ignore"):
+        flux = float(np.max(np.abs(fl - fl_ref) / np.where(fl_ref != 0, np.abs(fl_ref), 1.0)))
+        flux_all = float(np.max(np.abs(img.sum(axis=1) - ref.sum(axis=1)) / np.abs(ref.sum(axis=1))))
+    return {"rays": int(len(ref_steps)), "ill_conditioned": int(ill.sum()), "steps_equal": steps_equal,
+            "max_pixel_rel_err": max_pix, "flux_rel_err": flux, "flux_rel_err_all_rays": flux_all,
+            "max_pixel_rel_err_all_rays": float(err.max()), "bar": bar,
+            "ok": bool(steps_equal and max_pix <= bar and flux <= bar and ill.mean() < 0.05)}

@@ -1,9 +1,8 @@
 """Generate golden vectors by executing the UNMODIFIED reference (Mahakala).
 
-Run in a container that has the reference checkout (default
-``/root/reference``, override with ``MAHAKALA_REF``)::
+Run where the reference checkout exists, naming it in ``MAHAKALA_REF``::
 
-    python tests/golden/make_golden.py [name ...]
+    MAHAKALA_REF=<path to the Mahakala checkout> python tests/golden/make_golden.py [name ...]
 
 jax is not installable offline, so ``jaxshim.install()`` provides a NumPy
 stand-in for the jax subset the reference uses (see ``jaxshim.py``); the
@@ -35,7 +34,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("MAHAKALA_REF", "/root/reference")
+REF = os.environ.get("MAHAKALA_REF")
+if not REF or not os.path.isdir(os.path.join(REF, "mahakala")):
+    sys.exit("make_golden.py: set MAHAKALA_REF to the Mahakala checkout (the directory holding mahakala/)")
 
 sys.path.insert(0, HERE)
 sys.path.insert(0, REPO)

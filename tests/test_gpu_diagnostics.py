@@ -1,16 +1,17 @@
 """Per-step diagnostics from the fused FP64 render (images.step_diagnostics)
-against the reference's stage-by-stage sequence run through this package's
-stage kernels (images.py:56-144: geodesic_integrator, fluid scalars,
-electrons, synchrotron, sigma cut), then solve_specific_intensity(dIs=True)
-and solve_attenuated_emissivity (transfer.py:89-144) on both.
+against the oracle's stage-by-stage make_image sequence (images.py:56-120:
+geodesic_integrator, get_fluid_scalars_from_geodesics, beta/sigma,
+rlow_rhigh_model, units, synchrotron_coefficients, sigma cut), then
+solve_specific_intensity(dIs=True) and solve_attenuated_emissivity
+(transfer.py:89-144) on the oracle's rows.
 
-Bars (relative, floor 1e-6 of each array's maximum): dt rows within 1e-7
-and zero at the same rows; emissivity and absorptivity within 1e-7 at
-every row a ray reaches, zero beyond; dIs, the attenuated emissivity and
-the image within 1e-7.  The two integrators agree to
-~1e-13 per step (the fused kernel takes r from the metric evaluation, the
-stage one from radius_cal); near the photon ring that difference grows
-along the path, which the 1e-7 bar covers on this small case.
+Bar: 1e-8 relative (floor 1e-4 of each array's maximum) on every
+well-conditioned entry of the dt, emissivity, absorptivity, dIs and
+attenuated-emissivity rows and of the image, with the zero pattern of dt
+identical.  An entry is ill-conditioned when the oracle's own pipeline run
+from initial wavevectors changed by 1e-12 (oracle.perturbed) moves it by
+more than 1e-10, or changes the ray's step count (then the whole ray is);
+such entries must stay under 5 % of those compared.
 """
 
 import numpy as np
@@ -20,66 +21,90 @@ from conftest import rel_err
 
 pytestmark = pytest.mark.gpu
 
+BAR = 1e-8
+ILL = 1e-10
+FLOOR = 1e-4
 
-def _stage_rows(model, kw):
-    import mahakala_gb300 as ma
-    from mahakala_gb300.electrons import rlow_rhigh_model
-    a = model.bhspin
-    s0 = ma.initialize_geodesics_at_camera(a, kw["camera_inclination"], 1000, -kw["fov"] / 2., kw["fov"] / 2.,
-                                           kw["resolution"])
-    S, dt = ma.geodesic_integrator(kw["max_nsteps"], s0, 40, 1e-4, a)
-    fs = model.get_fluid_scalars_from_geodesics(S)
-    bsq = fs["b"] * fs["b"]
-    beta = fs["u"] * (model.fluid_gamma - 1.) / bsq / 0.5
-    sigma = bsq / fs["dens"]
-    theta = rlow_rhigh_model(fs["dens"], fs["u"], beta, r_high=kw["r_high"])
-    units = model.get_units(kw["M_bh"], kw["mass_scale"])
+
+def _oracle_rows(orc, snap, a, kw, s0):
+    """The oracle's em, ab, dt rows, dIs, attenuated emissivity and image of
+    the rays s0, in the order make_image computes them."""
+    S, dt = orc.geodesic_integrator(kw["max_nsteps"], s0, 40, 1e-4, a)
+    fs = snap.get_fluid_scalars_from_geodesics(S)
+    with np.errstate(all="ignore"):
+        bsq = fs["b"] * fs["b"]
+        beta = fs["u"] * (snap.fluid_gamma - 1.) / bsq / 0.5
+        sigma = bsq / fs["dens"]
+    theta = orc.rlow_rhigh_model(fs["dens"], fs["u"], beta, r_high=kw["r_high"])
+    units = orc.get_units(kw["M_bh"], kw["mass_scale"])
     nu = kw["observing_frequency"]
-    em, ab = ma.synchrotron_coefficients(units["Ne_unit"] * fs["dens"], theta, units["B_unit"] * fs["b"],
-                                         fs["pitch_angle"], -fs["kdotu"] * nu, invariant=True, rescale_nu=1. / nu)
+    em, ab = orc.synchrotron_coefficients(units["Ne_unit"] * fs["dens"], theta, units["B_unit"] * fs["b"],
+                                          fs["pitch_angle"], -fs["kdotu"] * nu, invariant=True, rescale_nu=1. / nu)
     cut = sigma > 100.
-    em = em.masked_fill(cut, 0.)
-    ab = ab.masked_fill(cut, 0.)
-    return em, ab, dt, units["L_unit"]
+    em = np.where(cut, 0., em)
+    ab = np.where(cut, 0., ab)
+    I, dIs = orc.solve_specific_intensity(em, ab, dt, units["L_unit"], dIs=True)
+    att = orc.solve_attenuated_emissivity(em, ab, dt, units["L_unit"])
+    K = orc.integrate(s0, kw["max_nsteps"], 40, 1e-4, a)["K"]
+    return dict(em=em, ab=ab, dt=dt, dIs=dIs, attenuated=att, image=I, K=K)
 
 
-def test_step_diagnostics_match_stage_sequence(cuda, tiny_arrays):
-    from mahakala_gb300 import transfer
+def _pad_rows(x, n):
+    """x with rows appended (zeros) up to n rows; the two runs may trim to
+    different lengths."""
+    if x.shape[0] >= n:
+        return x[:n]
+    return np.concatenate([x, np.zeros((n - x.shape[0],) + x.shape[1:])], axis=0)
+
+
+def test_step_diagnostics_match_oracle(cuda, orc, tiny_arrays):
     from mahakala_gb300.grmhd.athenak import AthenakFluidModel
     from mahakala_gb300.images import step_diagnostics
     model = AthenakFluidModel(tiny_arrays, tiny_arrays.bhspin, fluid_gamma=13. / 9)
     kw = dict(camera_inclination=60, mass_scale=1e27, M_bh=6.2e9 * 1.989e33, r_high=3, observing_frequency=230e9,
               fov=30, resolution=12, max_nsteps=1500)
     d = step_diagnostics(model, **kw)
-    em, ab, dt, L_unit = _stage_rows(model, kw)
-    em, ab, dt = em.cpu().numpy(), ab.cpu().numpy(), dt.cpu().numpy()
-    dem, dab, ddt = d["em"][0].cpu().numpy(), d["ab"][0].cpu().numpy(), d["dt"].cpu().numpy()
-    assert dem.shape == em.shape and ddt.shape == dt.shape
-    assert np.array_equal(ddt == 0, dt == 0)
-    assert np.max(rel_err(ddt, dt, floor=1e-6 * np.abs(dt).max())) <= 1e-7
+    a = tiny_arrays.bhspin
+    snap = orc.OracleSnapshot(tiny_arrays)
+    s0 = orc.initialize_geodesics_at_camera(a, kw["camera_inclination"], 1000, -kw["fov"] / 2., kw["fov"] / 2.,
+                                            kw["resolution"])
+    ref = _oracle_rows(orc, snap, a, kw, s0)
+    pert = _oracle_rows(orc, snap, a, kw, orc.perturbed(s0))
+    got = dict(em=d["em"][0].cpu().numpy(), ab=d["ab"][0].cpu().numpy(), dt=d["dt"].cpu().numpy(),
+               dIs=d["dIs"][0].cpu().numpy(), attenuated=d["attenuated"][0].cpu().numpy(),
+               image=d["image"][0].cpu().numpy().reshape(-1))
     K = d["nsteps"].reshape(-1).cpu().numpy()
-    reached = np.arange(em.shape[0])[:, None] <= K[None, :]
-    assert em.max() > 0
-    for got, ref in ((dem, em), (dab, ab)):
-        floor = 1e-6 * np.abs(ref).max()
-        assert np.max(rel_err(got[reached], ref[reached], floor=floor)) <= 1e-7
-        assert np.all(got[~reached] == 0.0)
-    I_ref, dIs_ref = transfer.solve_specific_intensity(transfer_input(em), transfer_input(ab), transfer_input(dt),
-                                                       L_unit, dIs=True)
-    att_ref = transfer.solve_attenuated_emissivity(transfer_input(em), transfer_input(ab), transfer_input(dt),
-                                                   L_unit).cpu().numpy()
-    dIs_ref = dIs_ref.cpu().numpy()
-    for got, ref in ((d["dIs"][0].cpu().numpy(), dIs_ref), (d["attenuated"][0].cpu().numpy(), att_ref)):
-        assert got.shape == ref.shape
-        assert np.max(rel_err(got, ref, floor=1e-6 * np.abs(ref).max())) <= 1e-7
-    img = d["image"][0].cpu().numpy().reshape(-1)
-    I_ref = I_ref.cpu().numpy()
-    assert np.max(rel_err(img, I_ref, floor=1e-6 * np.abs(I_ref).max())) <= 1e-7
-
-
-def transfer_input(a):
-    import torch
-    return torch.as_tensor(a, dtype=torch.float64, device="cuda")
+    assert ref["em"].max() > 0
+    # both runs keep max(K) + 2 rows (geodesics.py:275-281); only an
+    # ill-conditioned ray can make the two lengths differ
+    nrows = ref["em"].shape[0]
+    for key in ("dt", "em", "ab", "dIs", "attenuated"):
+        got[key] = _pad_rows(got[key], ref[key].shape[0])
+    ray_ill = pert["K"] != ref["K"]
+    assert np.array_equal(K[~ray_ill], ref["K"][~ray_ill])
+    assert np.array_equal(got["dt"][:, ~ray_ill] == 0, ref["dt"][:, ~ray_ill] == 0)
+    # rows the ray reached (later rows: the reference repeats the frozen
+    # state's sample with dt = 0, the fused kernel leaves zeros; the
+    # transfer weighs both by dt = 0)
+    reached = np.arange(nrows)[:, None] <= ref["K"][None, :]
+    compared, ill_total = 0, 0
+    for key in ("dt", "em", "ab", "dIs", "attenuated", "image"):
+        g, r = got[key], ref[key]
+        p = _pad_rows(pert[key], r.shape[0]) if key != "image" else pert[key]
+        floor = FLOOR * np.abs(r).max()
+        ill = (rel_err(p, r, floor=floor) > ILL) | ray_ill
+        if key in ("em", "ab"):
+            mask = reached & ~ill
+            ill = ill & reached
+        else:
+            mask = ~ill
+        err = rel_err(g, r, floor=floor)
+        assert np.max(err[mask], initial=0.0) <= BAR, (key, float(np.max(err[mask])))
+        compared += mask.sum() + ill.sum()
+        ill_total += ill.sum()
+        if key in ("em", "ab"):
+            assert np.all(g[~reached] == 0.0), key
+    assert ill_total < 0.05 * compared, f"{ill_total} of {compared} entries ill-conditioned"
 
 
 def test_step_diagnostics_multifrequency_rows_and_fp64_only(cuda, tiny_arrays):

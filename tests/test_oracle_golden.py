@@ -194,3 +194,24 @@ def test_multilevel_image_matches_reference(orc):
     ref = d["case0_image"]
     assert ref.max() > 0
     assert np.max(np.abs(img - ref)) / np.max(np.abs(ref)) < 1e-12
+
+
+def test_image_parity_checker_flags_planted_errors(orc, tiny_arrays):
+    """oracle.image_parity (the FP64 image checker of the benchmark and the
+    headline GPU test) passes the oracle against itself and fails an image
+    with a 1e-7 error planted in one conditioned pixel or one step count
+    changed."""
+    snap = orc.OracleSnapshot(tiny_arrays)
+    s0 = orc.initialize_geodesics_at_camera(0.9, 60, 1000, -15., 15., 8)
+    kw = dict(mass_scale=1e27, r_high=3, max_nsteps=1500)
+    img, steps = orc.render_rays(snap, s0, **kw)
+    pimg, psteps = orc.render_rays(snap, orc.perturbed(s0), **kw)
+    rep = orc.image_parity(img, steps, img, steps, pimg, psteps)
+    assert rep["ok"] and rep["max_pixel_rel_err"] == 0.0
+    k = int(np.argmax(img[0]))
+    bad = img.copy()
+    bad[0, k] *= 1 + 1e-7
+    assert not orc.image_parity(bad, steps, img, steps, pimg, psteps)["ok"]
+    bad_steps = steps.copy()
+    bad_steps[k] += 1
+    assert not orc.image_parity(img, bad_steps, img, steps, pimg, psteps)["ok"]
