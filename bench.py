@@ -376,12 +376,18 @@ def time_render(torch, prep, stream, steps, warmup, flush, barrier, min_warmup=3
     return [a.elapsed_time(b) * 1e-3 for a, b in ev], phases
 
 
-def run_serving(torch, model0, n, precisions):
+def run_serving(torch, model0, n, precisions, latency_bound=2.0):
     """Config-4 stream: Poisson arrivals at 20/s over two resident snapshots
     (seeds 0 and 1), mixed resolutions/spins/inclinations/frequencies/R_high,
     continuous batching over four CUDA-graph slots.  Per form: p50/p99
-    latency, served rays/s, and the p99 of each request's latency divided by
-    its isolated single-image render time."""
+    latency, served rays/s, the p99 of each request's latency divided by
+    its isolated single-image render time, and the offered load (the
+    requests' isolated render time summed over the arrival span: above 1
+    the GPU cannot keep up at that rate).  The same stream is served a
+    second time with latency-bound admission (requests that cannot finish
+    within latency_bound x their predicted isolated latency are shed; the
+    predictor is each resolution's latency served alone, calibrated on
+    separate requests before the stream)."""
     from mahakala_gb300 import configs
     from mahakala_gb300.grmhd.athenak import AthenakFluidModel
     from mahakala_gb300.serving import (DeviceExecutor, Scheduler, isolated_latencies, isolated_times,
@@ -395,12 +401,15 @@ def run_serving(torch, model0, n, precisions):
         arrivals, reqs = poisson_stream(models, n, rate_hz=c["rate_hz"], seed=c["seed"])
         ex = DeviceExecutor(models, precision=form, nslots=4)
         out["buckets"] = list(ex.buckets)
-        sched = Scheduler(ex, hbm_budget=ex.resident_bytes + (8 << 30))
+
+        def factory(**kw):
+            return Scheduler(ex, hbm_budget=ex.resident_bytes + (8 << 30), **kw)
+        sched = factory()
         torch.cuda.synchronize()
         tickets, wall = serve_stream(sched, arrivals, reqs)
         # isolated reference 1: each request served alone through the same
         # server path (graph replay, copies, polling)
-        iso_e2e = isolated_latencies(lambda: Scheduler(ex, hbm_budget=ex.resident_bytes + (8 << 30)), reqs)
+        iso_e2e = isolated_latencies(factory, reqs)
         rep = latency_report(tickets, wall, isolated={t.id: iso_e2e[i] for i, t in enumerate(tickets)})
         rep["isolated_ms_p50"] = 1e3 * float(np.percentile(iso_e2e, 50))
         rep["isolated_ms_p99"] = 1e3 * float(np.percentile(iso_e2e, 99))
@@ -411,13 +420,46 @@ def run_serving(torch, model0, n, precisions):
         rep["device_only"] = {"slowdown_p50": dev["slowdown_p50"], "slowdown_p99": dev["slowdown_p99"],
                               "isolated_ms_p50": 1e3 * float(np.percentile(iso, 50)),
                               "isolated_ms_p99": 1e3 * float(np.percentile(iso, 99))}
+        span = float(arrivals[-1])
+        rep["offered_load"] = sum(iso) / span
+        rep["offered_load_e2e"] = sum(iso_e2e) / span
+        rep["offered_load_note"] = ("sum of the requests' isolated render times (device; e2e: through the "
+                                    "server alone) over the arrival span: above 1 the GPU cannot keep up")
         rep["isolated_note"] = ("slowdown = stream latency / the same request's latency served alone through the "
                                 "same scheduler; device_only divides by its render kernels' time alone")
         rep["nonfinite_images"] = int(sum(not np.all(np.isfinite(t.image)) for t in tickets if t.image is not None))
         rep["batches"] = len(sched.batches)
         rep["mean_requests_per_batch"] = float(np.mean([b["requests"] for b in sched.batches]))
+        # latency-bound admission: calibrate a per-resolution predictor on
+        # requests that are not in the stream, then serve the stream again
+        _, cal = poisson_stream(models, 16, rate_hz=c["rate_hz"], seed=c["seed"] + 1)
+        by_res = {}
+        for r in cal:
+            by_res.setdefault(int(r.resolution), []).append(r)
+        table = {res: float(np.median(isolated_latencies(factory, rs[:2]))) for res, rs in by_res.items()}
+        known = sorted(table)
+
+        def predict(r):
+            res = int(r.resolution)
+            if res in table:
+                return table[res]
+            near = min(known, key=lambda k: abs(k - res))
+            return table[near] * (res / near) ** 2
+        bsched = factory(latency_bound=latency_bound, predict=predict)
+        torch.cuda.synchronize()
+        btickets, bwall = serve_stream(bsched, arrivals, reqs)
+        brep = latency_report(btickets, bwall, isolated={t.id: iso_e2e[i] for i, t in enumerate(btickets)})
+        served_iso = [iso_e2e[i] for i, t in enumerate(btickets) if t.status == "done"]
+        if served_iso:
+            brep["isolated_ms_p99"] = 1e3 * float(np.percentile(served_iso, 99))
+            brep["p99_over_isolated_p99"] = brep["p99_ms"] / brep["isolated_ms_p99"]
+        brep["latency_bound"] = latency_bound
+        brep["predictor_ms"] = {str(k): 1e3 * v for k, v in sorted(table.items())}
+        brep["note"] = ("requests predicted to miss latency_bound x their isolated latency are shed (status "
+                        "'shed', counted apart from served); p99 over the served requests")
+        rep["bounded"] = brep
         out[form] = rep
-        del ex, sched
+        del ex, sched, bsched
         torch.cuda.empty_cache()
     return out
 

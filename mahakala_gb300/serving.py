@@ -14,8 +14,16 @@ work overlaps on the device.
 Admission is by HBM budget: the snapshots and the slots' buffers are
 resident; a request is admitted when its output buffers fit in what the
 budget leaves, otherwise it waits; a request that can never fit (or that
-is malformed) is rejected at submission.  Latency is measured from
-arrival to the moment its image is in host memory.
+is malformed) is rejected at submission.  Optionally admission is also
+by latency: given a predictor of each request's latency when served alone
+and a factor k, a request whose predicted latency in the stream (the
+predicted work queued ahead of it plus its own) exceeds k times its
+isolated latency is shed at submission, and a waiting request that can no
+longer finish within k times its isolated latency is shed before launch.
+Shed requests end with status "shed" (reported as failures), so under an
+offered load above what the GPU can serve the served requests keep their
+latency bound instead of the queue growing without end.  Latency is
+measured from arrival to the moment its image is in host memory.
 
 The scheduling core (``Scheduler``) is plain Python over an executor
 interface, so its logic is tested on the CPU with a fake executor;
@@ -52,16 +60,17 @@ class Ticket:
     launched: float = None
     finished: float = None
     image: np.ndarray = None
-    status: str = "waiting"    # waiting | running | done | failed | cancelled
+    status: str = "waiting"    # waiting | running | done | failed | cancelled | shed
     error: str = None
     batch: int = None
+    predicted: float = None    # predicted latency served alone (s), with a latency bound
 
     @property
     def latency(self):
         return None if self.finished is None else self.finished - self.arrival
 
     def done(self):
-        return self.status in ("done", "failed", "cancelled")
+        return self.status in ("done", "failed", "cancelled", "shed")
 
 
 def validate(req, max_rays):
@@ -101,7 +110,17 @@ class Scheduler:
                       images=[...]) with one image per ticket
     """
 
-    def __init__(self, executor, hbm_budget, max_requests=MAX_REQUESTS_PER_BATCH, clock=time.perf_counter):
+    def __init__(self, executor, hbm_budget, max_requests=MAX_REQUESTS_PER_BATCH, clock=time.perf_counter,
+                 latency_bound=None, predict=None):
+        """latency_bound (k) with predict(request) -> seconds: shed requests
+        that cannot be served within k times their predicted isolated
+        latency (see the module docstring); None admits by budget only."""
+        if (latency_bound is None) != (predict is None):
+            raise ValueError("latency_bound and predict go together")
+        if latency_bound is not None and not latency_bound > 1.0:
+            raise ValueError("latency_bound must exceed 1")
+        self.latency_bound = latency_bound
+        self.predict = predict
         self.ex = executor
         self.budget = int(hbm_budget)
         self.max_requests = int(max_requests)
@@ -128,8 +147,35 @@ class Scheduler:
         t = Ticket(next(self._ids), req, int(req.resolution) ** 2, ob,
                    self.clock() if arrival is None else arrival)
         self.tickets.append(t)
+        if self.latency_bound is not None:
+            t.predicted = float(self.predict(req))
+            now = self.clock()
+            ahead = self.backlog(now)
+            if (now - t.arrival) + ahead + t.predicted > self.latency_bound * t.predicted:
+                self._shed(t, now, f"predicted latency {1e3 * (ahead + t.predicted):.1f} ms with "
+                                   f"{1e3 * ahead:.1f} ms of work ahead exceeds {self.latency_bound:g} x "
+                                   f"{1e3 * t.predicted:.1f} ms")
+                return t
         self.pending.append(t)
         return t
+
+    def _shed(self, t, now, why):
+        t.status, t.finished, t.error = "shed", now, "shed: " + why
+
+    def backlog(self, now):
+        """Predicted seconds of work queued ahead of a new arrival: what the
+        in-flight batches have left (predicted) plus every waiting request.
+        The GPU is one server: batches on several slots share it."""
+        if self.predict is None:
+            return 0.0
+        left = 0.0
+        for busy in self.slots:
+            if busy is None:
+                continue
+            _, _, tickets = busy
+            work = sum(t.predicted for t in tickets)
+            left += max(0.0, tickets[0].launched + work - now)
+        return left + sum(t.predicted for t in self.pending)
 
     def cancel(self, ticket):
         """Cancel a request that has not been launched yet."""
@@ -159,18 +205,36 @@ class Scheduler:
             self.slots[s] = None
 
     def _pack(self):
-        """FIFO requests that fit one bucket, the request cap and the budget."""
+        """FIFO requests that fit one bucket, the request cap and the budget.
+        With a latency bound, waiting requests that can no longer finish in
+        time are shed first, and a request joins the batch only if the
+        batch's predicted time (the sum of its members' predictions: one
+        batch returns all its images together) keeps every member within
+        its bound."""
+        bound = self.latency_bound
+        now = self.clock()
+        if bound is not None:
+            for t in list(self.pending):
+                if (now - t.arrival) + t.predicted > bound * t.predicted:
+                    self.pending.remove(t)
+                    self._shed(t, now, f"waited {1e3 * (now - t.arrival):.1f} ms, cannot finish within "
+                                       f"{bound:g} x {1e3 * t.predicted:.1f} ms")
         cap = max(self.ex.buckets)
-        batch, rays, nbytes = [], 0, 0
+        batch, rays, nbytes, work = [], 0, 0, 0.0
         free = self.free_bytes
         for t in list(self.pending):
             if len(batch) >= self.max_requests or rays + t.rays > cap:
                 break
             if nbytes + t.out_bytes > free:
                 break
+            if bound is not None and batch:
+                w = work + t.predicted
+                if any((now - m.arrival) + w > bound * m.predicted for m in batch + [t]):
+                    continue  # waits for a batch of its own
             batch.append(t)
             rays += t.rays
             nbytes += t.out_bytes
+            work += t.predicted or 0.0
         return batch, rays
 
     def step(self):
@@ -253,6 +317,7 @@ def latency_report(tickets, wall, isolated=None):
     lat = np.array([t.latency for t in done])
     rays = sum(t.rays for t in done)
     out = dict(requests=len(tickets), served=len(done), failed=sum(t.status == "failed" for t in tickets),
+               shed=sum(t.status == "shed" for t in tickets),
                p50_ms=1e3 * float(np.percentile(lat, 50)) if len(lat) else None,
                p99_ms=1e3 * float(np.percentile(lat, 99)) if len(lat) else None,
                max_ms=1e3 * float(lat.max()) if len(lat) else None,

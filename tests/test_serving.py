@@ -164,3 +164,77 @@ def test_request_cap_per_batch():
         s.submit(req(4))
     drive(s, clock)
     assert [len(ids) for _, _, ids in ex.launches] == [4, 4, 2]
+
+
+def _overload(clock, latency_bound):
+    """An arrival every 0.05 s of requests that each take 0.1 s alone on a
+    one-slot executor (offered load 2), served with or without a latency
+    bound."""
+    ex = FakeExecutor(clock, nslots=1, buckets=(100, 400, 1600), cost=1e-3)
+    kw = {} if latency_bound is None else dict(latency_bound=latency_bound,
+                                               predict=lambda r: 1e-3 * int(r.resolution) ** 2)
+    s = Scheduler(ex, hbm_budget=10 ** 9, clock=clock, **kw)
+    tickets = []
+    for k in range(40):
+        while clock.t < 0.05 * k:
+            s.step()
+            clock.t += 1e-3
+        tickets.append(s.submit(req(10), arrival=clock.t))
+    drive(s, clock, until=1000.0)
+    return tickets
+
+
+def test_latency_bound_sheds_under_overload_and_bounds_served_latency():
+    """Offered load 2: without a bound every request is served and the
+    queue (and latency) grows; with k = 2, some requests are shed and every
+    served one finishes within 2x its isolated time (plus the 1 ms poll
+    step of the fake clock)."""
+    free = _overload(Clock(), None)
+    assert all(t.status == "done" for t in free)
+    assert max(t.latency for t in free) > 10 * 0.1
+    bounded = _overload(Clock(), 2.0)
+    served = [t for t in bounded if t.status == "done"]
+    shed = [t for t in bounded if t.status == "shed"]
+    assert served and shed and len(served) + len(shed) == len(bounded)
+    assert all(t.latency <= 2.0 * 0.1 + 2e-3 for t in served), max(t.latency for t in served)
+    assert all(t.error.startswith("shed") for t in shed)
+    rep = latency_report(bounded, 3.0)
+    assert rep["shed"] == len(shed) and rep["served"] == len(served)
+
+
+def test_latency_bound_admits_everything_under_light_load():
+    clock = Clock()
+    ex = FakeExecutor(clock, cost=1e-3)
+    s = Scheduler(ex, hbm_budget=10 ** 9, clock=clock, latency_bound=2.0,
+                  predict=lambda r: 1e-3 * int(r.resolution) ** 2)
+    tickets = []
+    for k in range(10):
+        while clock.t < 0.5 * k:
+            s.step()
+            clock.t += 1e-3
+        tickets.append(s.submit(req(10), arrival=clock.t))
+    drive(s, clock)
+    assert all(t.status == "done" for t in tickets)
+
+
+def test_latency_bound_keeps_batches_within_every_members_bound():
+    """A small request is not packed behind a large one when the batch's
+    predicted time would break the small one's bound."""
+    clock = Clock()
+    ex = FakeExecutor(clock, nslots=1, buckets=(100, 400, 1600), cost=1e-3)
+    s = Scheduler(ex, hbm_budget=10 ** 9, clock=clock, latency_bound=2.0,
+                  predict=lambda r: 1e-3 * int(r.resolution) ** 2)
+    big = s.submit(req(30))      # 0.9 s
+    small = s.submit(req(4))     # 0.016 s: would wait for the big one's 0.9 s
+    s.step()
+    assert ex.launches[0][2] == [big.id]
+    drive(s, clock)
+    assert big.status == "done" and small.status == "shed"
+
+
+def test_latency_bound_needs_a_predictor():
+    clock = Clock()
+    with pytest.raises(ValueError):
+        Scheduler(FakeExecutor(clock), hbm_budget=10 ** 9, clock=clock, latency_bound=2.0)
+    with pytest.raises(ValueError):
+        Scheduler(FakeExecutor(clock), hbm_budget=10 ** 9, clock=clock, latency_bound=1.0, predict=lambda r: 1.0)
