@@ -388,6 +388,16 @@ int mk_render_phase_ms(float *ms_out, int32_t *nphases);
 int mk_probe_fma(int32_t precision, int32_t blocks, int32_t threads, int64_t iters, void *out_dev,
                  void *stream);
 
+/* The FP64 path's own reciprocal square root, reciprocal and square root
+   (float-unit seed refined by one third-order correction in binary64;
+   no reference counterpart) and, for comparison, the library's correctly
+   rounded forms, applied to x_dev (n) -> out_dev (n). */
+typedef enum {
+    MK_MATH_RSQRT = 0, MK_MATH_RCP = 1, MK_MATH_SQRT = 2,
+    MK_MATH_LIB_RSQRT = 3, MK_MATH_LIB_RCP = 4, MK_MATH_LIB_SQRT = 5
+} mk_math_fn;
+int mk_probe_math(int32_t fn, const double *x_dev, int64_t n, double *out_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,7 @@ MK_POLICY_REFERENCE, MK_POLICY_FIXED = 0, 1
 MK_CAMERA_GRID, MK_CAMERA_EQUATOR = 0, 1
 MK_MAX_NU = 4
 MK_PROBE_FFMA2 = 100
+MK_MATH_RSQRT, MK_MATH_RCP, MK_MATH_SQRT, MK_MATH_LIB_RSQRT, MK_MATH_LIB_RCP, MK_MATH_LIB_SQRT = range(6)
 NOALLOC_WORKSPACE_BYTES = 16 << 20
 NOALLOC_MAX_MIXED_RAYS = (NOALLOC_WORKSPACE_BYTES - 256) // 320
 MK_WS_STEPS, MK_WS_SAMPLES, MK_WS_MAX_TAU, MK_WS_TO_FP64, MK_WS_FP32_QUEUE, MK_WS_STEPS_FP64 = 1, 2, 3, 4, 6, 8
@@ -110,6 +111,7 @@ SIGNATURES = {
     "mk_render_job": (_c.c_int, [_VP, _VP, _VP, _I32, _I64, _VP, _SZ, _VP]),
     "mk_sizeof": (_SZ, [_c.c_char_p]),
     "mk_probe_fma": (_c.c_int, [_I32, _I32, _I32, _I64, _VP, _VP]),
+    "mk_probe_math": (_c.c_int, [_I32, _VP, _I64, _VP, _VP]),
     "mk_set_tuning": (_c.c_int, [_c.c_char_p, _I64]),
     "mk_render_phase_ms": (_c.c_int, [_VP, _VP]),
 }

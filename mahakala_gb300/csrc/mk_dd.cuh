@@ -76,9 +76,70 @@ __host__ __device__ __forceinline__ dd inv_sqrt(dd x) {
     return yy + yy * e * dd(0.5f, 0.0f);
 }
 
+// ------------------------------------------------------------------------
+// Binary64 reciprocal square root and reciprocal for the FP64 path, whose
+// time is its FP64-pipe instruction count (1/64 of the FP32 rate on this
+// part).  The seed is the float unit's approximation (rsqrtf, __fdividef)
+// of the argument moved to float and back by bit operations on the integer
+// pipe -- exponent rebased between the two formats, significand truncated
+// to 23 bits -- so only the correction runs on the FP64 pipe.  One
+// third-order correction (Householder's method of order 3: the binomial
+// series (1 - e)^(-1/2) = 1 + e/2 + 3e^2/8 + O(e^3) and (1 - e)^(-1) =
+// 1 + e + e^2 + O(e^3), e the seed's residual, |e| < 2^-20) leaves a
+// truncation below 2^-58; with the correction's own roundings the result
+// is within 2 ulp of the exact value (tests/test_gpu_math.py checks it
+// against the correctly rounded library forms).  Arguments whose binary
+// exponent lies outside [-120, 119] -- zero, subnormals, negative values,
+// infinities and NaN included -- take the library forms.
+
+// |x| with biased exponent in [903, 1142] -> float with the same value,
+// significand truncated (positive x only)
+__device__ __forceinline__ float f32_bits_of(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    return __uint_as_float(((hi - (896u << 20)) << 3) | (lo >> 29));
+}
+
+// positive normal float -> the same value as a double, with the sign bit
+// `sign` (0 or 0x80000000)
+__device__ __forceinline__ double f64_bits_of(float y, unsigned sign = 0u) {
+    const unsigned u = __float_as_uint(y);
+    return __hiloint2double((int)(((u >> 3) + (896u << 20)) | sign), (int)(u << 29));
+}
+
+// biased exponent of the high word hi (sign included) in [903, 1142]
+__device__ __forceinline__ bool f64_seed_range(unsigned hi) { return (hi >> 20) - 903u <= 239u; }
+
+__device__ __forceinline__ double rsqrt64(double x) {
+    if (f64_seed_range((unsigned)((unsigned long long)__double_as_longlong(x) >> 32))) {
+        const double y = f64_bits_of(rsqrtf(f32_bits_of(x)));
+        const double e = fma(-(x * y), y, 1.0);          // 1 - x y^2
+        return fma(y * e, fma(0.375, e, 0.5), y);        // y (1 + e/2 + 3e^2/8)
+    }
+    return 1.0 / sqrt(x);
+}
+
+// sqrt(x) = x / sqrt(x), from rsqrt64 where its seed applies (exact
+// library form elsewhere: zero, subnormals, infinities, NaN)
+__device__ __forceinline__ double sqrt64(double x) {
+    if (f64_seed_range((unsigned)((unsigned long long)__double_as_longlong(x) >> 32))) return x * rsqrt64(x);
+    return sqrt(x);
+}
+
+__device__ __forceinline__ double rcp64(double d) {
+    const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(d) >> 32);
+    if (f64_seed_range(hi & 0x7fffffffu)) {
+        const double a = __hiloint2double((int)(hi & 0x7fffffffu), __double2loint(d));  // |d|
+        const double y = f64_bits_of(__fdividef(1.0f, f32_bits_of(a)), hi & 0x80000000u);
+        const double e = fma(-d, y, 1.0);                  // 1 - d y
+        return fma(y, fma(e, e, e), y);                    // y (1 + e + e^2)
+    }
+    return 1.0 / d;
+}
+
 // 1/sqrt for each arithmetic the geodesic code is instantiated with
 __device__ __forceinline__ float inv_sqrt(float x) { return rsqrtf(x); }
-__device__ __forceinline__ double inv_sqrt(double x) { return ::rsqrt(x); }
+__device__ __forceinline__ double inv_sqrt(double x) { return rsqrt64(x); }
 
 __host__ __device__ __forceinline__ double to_double(dd x) { return x.to_double(); }
 __host__ __device__ __forceinline__ double to_double(double x) { return x; }

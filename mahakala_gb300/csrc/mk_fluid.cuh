@@ -186,20 +186,25 @@ struct FluidFrame {
 __device__ __forceinline__ FluidFrame fluid_frame_m(const double prim[8], const KerrPoint<double> &m,
                                                     const double k[4], double cos_fallback) {
     const double f = m.f, l1 = m.l1, l2 = m.l2, l3 = m.l3;
-    // g^{00} = -1 - f, g^{0i} = f l_i
-    const double alpha = sqrt(1.0 / (1.0 + f));
+    // g^{00} = -1 - f, g^{0i} = f l_i; the lapse alpha = 1/sqrt(1 + f), the
+    // Lorentz factor gamma = sqrt(G), and 1/u^0 = alpha/gamma from the two
+    // reciprocal square roots (no division on the FP64 pipe)
+    const double opf = 1.0 + f;
+    const double alpha = rsqrt64(opf);
     const double U1 = prim[1], U2 = prim[2], U3 = prim[3];
     const double lU = l1 * U1 + l2 * U2 + l3 * U3;
-    const double gamma = sqrt(1.0 + ((U1 * U1 + U2 * U2 + U3 * U3) + f * lU * lU));
+    const double G = 1.0 + ((U1 * U1 + U2 * U2 + U3 * U3) + f * lU * lU);
+    const double rG = rsqrt64(G);
+    const double gamma = G * rG;
     const double ga_f = gamma * alpha * f;
-    const double uc0 = gamma / alpha;
+    const double uc0 = gamma * (opf * alpha);
     const double uc1 = U1 - ga_f * l1, uc2 = U2 - ga_f * l2, uc3 = U3 - ga_f * l3;
     const double lu = uc0 + l1 * uc1 + l2 * uc2 + l3 * uc3;
     const double flu = f * lu;
     const double ud0 = -uc0 + flu, ud1 = uc1 + l1 * flu, ud2 = uc2 + l2 * flu, ud3 = uc3 + l3 * flu;
     const double B1 = prim[5], B2 = prim[6], B3 = prim[7];
     const double bc0 = B1 * ud1 + B2 * ud2 + B3 * ud3;
-    const double iuc0 = 1.0 / uc0;
+    const double iuc0 = alpha * rG;
     const double bc1 = (B1 + uc1 * bc0) * iuc0, bc2 = (B2 + uc2 * bc0) * iuc0, bc3 = (B3 + uc3 * bc0) * iuc0;
     const double lb = bc0 + l1 * bc1 + l2 * bc2 + l3 * bc3;
     const double flb = f * lb;
@@ -208,13 +213,13 @@ __device__ __forceinline__ FluidFrame fluid_frame_m(const double prim[8], const 
     o.kdotu = k[0] * ud0 + k[1] * ud1 + k[2] * ud2 + k[3] * ud3;
     const double kdotb = k[0] * bd0 + k[1] * bd1 + k[2] * bd2 + k[3] * bd3;
     const double bdotb = bc0 * bd0 + bc1 * bd1 + bc2 * bd2 + bc3 * bd3;
-    double pitch = kdotb / (fabs(o.kdotu) * sqrt(bdotb));
+    o.b = sqrt64(bdotb);
+    double pitch = kdotb * rcp64(fabs(o.kdotu) * o.b);
     if (isnan(pitch)) pitch = cos_fallback;
-    if (fabs(pitch) > 1.0) pitch = pitch / fabs(pitch);
+    if (fabs(pitch) > 1.0) pitch = isinf(pitch) ? nan("") : copysign(1.0, pitch);  // x/|x|, inf/inf = NaN
     o.cos_pitch = pitch;
     o.dens = prim[0];
     o.u = prim[4];
-    o.b = sqrt(bdotb);
     return o;
 }
 
@@ -231,6 +236,17 @@ __device__ __forceinline__ FluidScalars fluid_frame(const double prim[8], double
 }
 
 // rlow_rhigh_model (electrons.py:32-50)
+// the same with reciprocals in place of the three divisions (the fused
+// FP64 render: within a few ulp of rlow_rhigh, which the stage kernel
+// keeps bit-exact to the reference)
+__device__ __forceinline__ double rlow_rhigh_fast(double dens, double u, double beta, double r_low,
+                                                  double r_high, double gem1, double gim1) {
+    const double b2 = beta * beta;
+    const double T_ratio = (r_high * b2 + r_low) * rcp64(1.0 + b2);
+    const double t = CL2 * (((MP * u) * gem1) * gim1);
+    return t * rcp64(dens * (gim1 + gem1 * T_ratio)) * (1.0 / ME_CL_CL);
+}
+
 __device__ __forceinline__ double rlow_rhigh(double dens, double u, double beta, double r_low,
                                              double r_high, double gem1, double gim1) {
     const double b2 = beta * beta;
@@ -242,17 +258,23 @@ __device__ __forceinline__ double rlow_rhigh(double dens, double u, double beta,
 
 // synchrotron_coefficients (transfer.py:30-86), FP64.  Frequency-independent
 // parts are split out so a multi-frequency pass evaluates them once.
+// per-sample factors of the synchrotron fit shared by every frequency:
+// nus, Theta_e, Ne, and the reciprocals 1/nus, 1/(2 Theta_e^2), 1/Theta_e
+// (quotients become products on the FP64 pipe; each within 2 ulp)
 struct SynchroPre {
-    double nus, th, Ne, th2;
+    double nus, th, Ne, inus, i2th2, ith;
 };
 
 __device__ __forceinline__ SynchroPre synchro_pre_sin(double Ne, double Th, double B, double sin_pitch) {
     SynchroPre p;
-    const double nuc = EE * B / TWO_PI_ME_CL;
-    p.th2 = Th * Th;
-    p.nus = ((TWO_NINTHS * nuc) * p.th2) * sin_pitch;
+    const double nuc = B * (EE / TWO_PI_ME_CL);
+    const double th2 = Th * Th;
+    p.nus = ((TWO_NINTHS * nuc) * th2) * sin_pitch;
     p.th = Th;
     p.Ne = Ne;
+    p.inus = rcp64(p.nus);
+    p.i2th2 = rcp64(2.0 * th2);
+    p.ith = rcp64(Th);
     return p;
 }
 
@@ -266,23 +288,25 @@ __device__ __forceinline__ double sin_from_cos(double c) { return sqrt((1.0 - c)
 
 __device__ __forceinline__ void synchro_eval(const SynchroPre &p, double nu, bool invariant, double rescale_nu,
                                              double &em_out, double &ab_out) {
-    const double X = nu / p.nus;
+    const double X = nu * p.inus;
     // X^(1/3) and X^(1/6) = sqrt(X^(1/3)): cbrt is exact to an ulp and far
     // cheaper than pow on the FP64 pipe
     const double x3 = cbrt(X);
     const double var = exp(-x3);
-    const double term = sqrt(X) + C2_11_12 * sqrt(x3);
-    double em = p.Ne * p.nus * (term * term) / (2.0 * p.th2);
-    em = em * var * SQRT2 * PI * EE2 / THREE_CL;
+    const double term = sqrt64(X) + C2_11_12 * sqrt64(x3);
+    double em = p.Ne * p.nus * (term * term) * p.i2th2;
+    em = em * var * (SQRT2 * PI * EE2 / THREE_CL);
     if (X > 1.e12) em = 0.0;
     if (p.th < 0.3) em = 0.0;
-    const double bx = HPL * nu / (ME_CL_CL * p.th);
-    const double Bden = (bx < 2.e-3) ? bx / 24. * (24. + bx * (12. + bx * (4. + bx))) : (exp(bx) - 1.0);
-    const double Bnu = (TWO_HPL * (nu * nu * nu) / Bden) / CL2;
-    double ab = em / Bnu;
+    const double bx = (HPL / ME_CL_CL) * nu * p.ith;
+    const double Bden = (bx < 2.e-3) ? bx * (1.0 / 24.) * (24. + bx * (12. + bx * (4. + bx))) : (exp(bx) - 1.0);
+    // alpha = em / B_nu with B_nu = 2 HPL nu^3 / Bden / CL^2
+    const double inu = rcp64(nu);
+    double ab = em * Bden * (CL2 / TWO_HPL) * (inu * inu * inu);
     if (invariant) {
         const double rn = nu * rescale_nu;
-        em = em / (rn * rn);
+        const double irn = rcp64(rn);
+        em = em * (irn * irn);
         ab = ab * rn;
     }
     em_out = isnan(em) ? 0.0 : em;

@@ -65,13 +65,14 @@ __host__ __device__ constexpr dd sixth<dd>() { return dd(0x1.555556p-3f, -0x1.55
 // exact small constants in the arithmetic code are written as float
 // literals (0.5f, 2.0f, ...): the same value in double, float and pairs
 
-// Quotient for each arithmetic: binary64 and pairs divide exactly; the float
-// (mixed-form) paths take the hardware reciprocal (__fdividef: ~2 ulp, two
-// instructions instead of a division subroutine; |y| stays far below 2^126
-// here -- the largest divisor, (r^4 + a^2 z^2)(r^2 + a^2) at the camera, is
-// ~1e18).
+// Quotient for each arithmetic: pairs divide exactly; binary64 multiplies
+// by rcp64's reciprocal (within 2 ulp; the division subroutine costs the
+// FP64 pipe several times more); the float (mixed-form) paths take the
+// hardware reciprocal (__fdividef: ~2 ulp, two instructions instead of a
+// division subroutine; |y| stays far below 2^126 here -- the largest
+// divisor, (r^4 + a^2 z^2)(r^2 + a^2) at the camera, is ~1e18).
 __device__ __forceinline__ float fdiv(float x, float y) { return __fdividef(x, y); }
-__device__ __forceinline__ double fdiv(double x, double y) { return x / y; }
+__device__ __forceinline__ double fdiv(double x, double y) { return x * rcp64(y); }
 __device__ __forceinline__ dd fdiv(dd x, dd y) { return x / y; }
 
 // Kerr-Schild metric data at a point: g = eta + f l l
@@ -256,32 +257,40 @@ __device__ __forceinline__ void kerr_accel(T x, T y, T z, T k0, T k1, T k2, T k3
 }
 
 // RK4 step whose first-stage acceleration d1 (at s) is already known; the
-// other three stages are evaluated here.
+// other three stages are evaluated here.  With F = (k, accel) the state's
+// derivative, the stages sit at s + h F1, s + h F2 (h = dt/2) and s + dt F3
+// and out = s + dt/6 (F1 + 2 F2 + 2 F3 + F4): the reference's
+// k_i = dt F_i, s + k/2 and (k1 + 2k2 + 2k3 + k4)/6 (geodesics.py:317-336)
+// with dt folded into the coefficients -- one fused multiply-add per
+// component and stage instead of a product and a sum (the FP64 form is
+// bound by its FP64 instruction count), equal to rounding.
 template <typename T>
 __device__ __forceinline__ void rk4_step_k1(const T s[8], const T d1[4], T dt, T a, T out[8]) {
+    const T h = T(0.5f) * dt;
     T acc[8], tmp[8], d0, dd1, d2, d3;
     {
-        const T k[8] = {dt * s[4], dt * s[5], dt * s[6], dt * s[7], dt * d1[0], dt * d1[1], dt * d1[2], dt * d1[3]};
+        const T F[8] = {s[4], s[5], s[6], s[7], d1[0], d1[1], d1[2], d1[3]};
 #pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = k[i]; tmp[i] = s[i] + T(0.5f) * k[i]; }
+        for (int i = 0; i < 8; i++) { acc[i] = F[i]; tmp[i] = s[i] + h * F[i]; }
     }
     kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
     {
-        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
+        const T F[8] = {tmp[4], tmp[5], tmp[6], tmp[7], d0, dd1, d2, d3};
 #pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2.0f) * k[i]; tmp[i] = s[i] + T(0.5f) * k[i]; }
+        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2.0f) * F[i]; tmp[i] = s[i] + h * F[i]; }
     }
     kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
     {
-        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
+        const T F[8] = {tmp[4], tmp[5], tmp[6], tmp[7], d0, dd1, d2, d3};
 #pragma unroll
-        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2.0f) * k[i]; tmp[i] = s[i] + k[i]; }
+        for (int i = 0; i < 8; i++) { acc[i] = acc[i] + T(2.0f) * F[i]; tmp[i] = s[i] + dt * F[i]; }
     }
     kerr_accel(tmp[1], tmp[2], tmp[3], tmp[4], tmp[5], tmp[6], tmp[7], a, d0, dd1, d2, d3);
     {
-        const T k[8] = {dt * tmp[4], dt * tmp[5], dt * tmp[6], dt * tmp[7], dt * d0, dt * dd1, dt * d2, dt * d3};
+        const T F[8] = {tmp[4], tmp[5], tmp[6], tmp[7], d0, dd1, d2, d3};
+        const T c = dt * sixth<T>();
 #pragma unroll
-        for (int i = 0; i < 8; i++) out[i] = s[i] + sixth<T>() * (acc[i] + k[i]);
+        for (int i = 0; i < 8; i++) out[i] = s[i] + c * (acc[i] + F[i]);
     }
 }
 

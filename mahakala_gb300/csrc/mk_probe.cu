@@ -7,6 +7,7 @@
 // (two FMAs per instruction), which shows whether the FP32 figure was
 // bound by issue or by the pipe.
 #include "mk_common.cuh"
+#include "mk_dd.cuh"
 
 namespace mk {
 
@@ -41,9 +42,38 @@ __global__ void ffma2_probe_kernel(int iters, float seed, float *out) {
     if (s == -12345.0f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// the FP64 path's reciprocal square root, reciprocal and square root beside
+// the library's correctly rounded forms, element by element
+__global__ void math_probe_kernel(int fn, const double *__restrict__ x, long long n, double *__restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        double r;
+        switch (fn) {
+            case MK_MATH_RSQRT: r = rsqrt64(v); break;
+            case MK_MATH_RCP: r = rcp64(v); break;
+            case MK_MATH_SQRT: r = sqrt64(v); break;
+            case MK_MATH_LIB_RSQRT: r = 1.0 / __dsqrt_rn(v); break;
+            case MK_MATH_LIB_RCP: r = __drcp_rn(v); break;
+            default: r = __dsqrt_rn(v); break;
+        }
+        out[i] = r;
+    }
+}
+
 }  // namespace mk
 
 using namespace mk;
+
+extern "C" int mk_probe_math(int32_t fn, const double *x_dev, int64_t n, double *out_dev, void *stream) {
+    MK_REQUIRE(fn >= MK_MATH_RSQRT && fn <= MK_MATH_LIB_SQRT, MK_ERR_ARG, "mk_probe_math: unknown function %d",
+               (int)fn);
+    MK_REQUIRE(n >= 0 && (n == 0 || (x_dev && out_dev)), MK_ERR_ARG, "mk_probe_math: bad arguments");
+    if (n == 0) return MK_OK;
+    math_probe_kernel<<<grid_for(n < 65536 ? n : 65536, 256), 256, 0, as_stream(stream)>>>(fn, x_dev, (long long)n,
+                                                                                           out_dev);
+    MK_LAUNCHED("math_probe_kernel");
+    return MK_OK;
+}
 
 // Launches the probe: blocks x threads threads, iters x 8 FMAs each (x 16
 // for MK_PROBE_FFMA2).  kind: MK_FP64, MK_MIXED (= FP32) or MK_PROBE_FFMA2.

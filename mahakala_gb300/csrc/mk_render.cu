@@ -244,10 +244,12 @@ __device__ __forceinline__ void sample_fp64(const mk_request &R, const mk_snapsh
     trilinear8(sv, c, prim);
     const FluidFrame fs = fluid_frame_m(prim, m, s + 4, R.cos_fallback_pitch);
     // derived quantities (images.py:87-102)
+    // quotients as products with rcp64 reciprocals (within a few ulp of the
+    // reference's divisions; the FP64 pipe is this kernel's bound)
     const double bsq = fs.b * fs.b;
-    const double beta = fs.u * (R.fluid_gamma - 1.) / bsq / 0.5;
-    const double sigma = bsq / fs.dens;
-    const double Th = rlow_rhigh(fs.dens, fs.u, beta, R.r_low, R.r_high, R.electron_gamma_m1, R.ion_gamma_m1);
+    const double beta = fs.u * (R.fluid_gamma - 1.) * 2.0 * rcp64(bsq);
+    const double sigma = bsq * rcp64(fs.dens);
+    const double Th = rlow_rhigh_fast(fs.dens, fs.u, beta, R.r_low, R.r_high, R.electron_gamma_m1, R.ion_gamma_m1);
     const SynchroPre sp = synchro_pre_sin(R.Ne_unit * fs.dens, Th, R.B_unit * fs.b, sin_from_cos(fs.cos_pitch));
     const double w = -dt_used * R.L_unit;
     const bool cut = sigma > R.sigma_cut;  // images.py:116-118
@@ -256,7 +258,7 @@ __device__ __forceinline__ void sample_fp64(const mk_request &R, const mk_snapsh
         if (ch < R.nnu) {
             const double nu_obs = R.nu[ch];
             double em, ab;
-            synchro_eval(sp, -fs.kdotu * nu_obs, true, 1. / nu_obs, em, ab);
+            synchro_eval(sp, -fs.kdotu * nu_obs, true, rcp64(nu_obs), em, ab);
             if (cut) { em = 0.0; ab = 0.0; }
             if (row >= 0) {
                 const int64_t at = (ch * R.rows + row) * request_pixels(R.camera) + pix;
@@ -679,7 +681,6 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
     const long long total = min((long long)*(volatile unsigned long long *)&ws->q64_count, capacity);
     bool active = false, exhausted = false;
     int rq = 0, steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0, b_steps = 0;
-    long long ray = 0;
     // float-pair state (X, K) throughout, as in the FP32 phases; near the
     // hole the wavevector is renormalised to null in binary64 on entry, at
     // every radial turning point and on the way out.  After the ray leaves
@@ -703,7 +704,6 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             double s[8];
 #pragma unroll
             for (int i = 0; i < 8; i++) s[i] = q.s[i];
-            ray = q.ray;
             steps = q.steps;
             rq = q.rq;
             const mk_request &R = reqs[rq];
