@@ -34,7 +34,8 @@ __device__ __forceinline__ int find_block(const mk_snapshot_view &s, double x, d
     int c[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const double u = floor((xs[a] - s.lo[a]) / s.width[a]);
+        // candidate table cell (the face tests below decide exactly)
+        const double u = floor((xs[a] - s.lo[a]) * rcp64(s.width[a]));
         if (!(u >= -1.0 && u <= (double)s.nb[a])) return -1;  // far outside (or NaN)
         c[a] = (int)u < 0 ? 0 : ((int)u >= s.nb[a] ? s.nb[a] - 1 : (int)u);
     }
@@ -118,12 +119,38 @@ __device__ __forceinline__ bool locate(const mk_snapshot_view &s, double x, doub
     return true;
 }
 
+// locate for the fused FP64 render: the same block (find_block), the cell
+// index and offset from q = t / d taken as t * rcp64(d) and split by floor.
+// Where that differs from the reference's quotient (by an ulp, at a cell
+// edge) it picks the neighbouring cell with the offset at the other end,
+// and trilinear interpolation, continuous across cells, gives the same
+// value to rounding; the stage kernels keep locate's exact arithmetic.
+__device__ __forceinline__ bool locate_fast(const mk_snapshot_view &s, double x, double y, double z, CellPos &c) {
+    const int mb = find_block(s, x, y, z);
+    if (mb < 0) return false;
+    c.mb = mb;
+    const double *g = s.geom + 6 * (int64_t)mb;
+    const double xs[3] = {x, y, z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double d = __ldg(g + 3 + a);
+        const double q = (xs[a] - __ldg(g + a) + d) * rcp64(d);
+        const double fl = floor(q);
+        c.del[a] = q - fl;
+        const int i = (int)fl;
+        // the face test guarantees 0 <= i <= n up to rounding; clamp keeps loads in bounds
+        c.idx[a] = i < 0 ? 0 : (i > s.n ? s.n : i);
+    }
+    return true;
+}
+
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
 // trilinear interpolation of the 8 primitives (athenak.py:737-752), FP64.
 // Blocks whose ghosts average finer cells are read from their binary64 copy
 // (the means are not float32 values; the reference holds them in float64).
-__device__ __forceinline__ void trilinear8(const mk_snapshot_view &s, const CellPos &c, double prim[8]) {
+template <bool EXACT>
+__device__ __forceinline__ void trilinear8_impl(const mk_snapshot_view &s, const CellPos &c, double prim[8]) {
     const int n2 = s.n + 2;
     const int64_t sj = (int64_t)n2 * 8, sk = (int64_t)n2 * n2 * 8;
     const int64_t at = ((((int64_t)c.mb * n2 + c.idx[2]) * n2 + c.idx[1]) * n2 + c.idx[0]) * 8;
@@ -155,9 +182,12 @@ __device__ __forceinline__ void trilinear8(const mk_snapshot_view &s, const Cell
                 }
     }
     const double d1 = c.del[0], d2 = c.del[1], d3 = c.del[2];
-    // a + (b - a) d rounded twice (no fused multiply-add), as the reference
-    // evaluates it, so the interpolated primitives are bit-identical
-    auto lerp = [](double a, double b, double d) { return __dadd_rn(a, __dmul_rn(__dsub_rn(b, a), d)); };
+    // EXACT: a + (b - a) d rounded twice (no fused multiply-add), as the
+    // reference evaluates it, so the interpolated primitives are
+    // bit-identical; otherwise (fused render) one fused multiply-add
+    auto lerp = [](double a, double b, double d) {
+        return EXACT ? __dadd_rn(a, __dmul_rn(__dsub_rn(b, a), d)) : fma(b - a, d, a);
+    };
 #pragma unroll
     for (int p = 0; p < 8; p++) {
         const double aaa = v[0][0][0][p], aab = v[0][0][1][p], aba = v[0][1][0][p], abb = v[0][1][1][p];
@@ -170,6 +200,13 @@ __device__ __forceinline__ void trilinear8(const mk_snapshot_view &s, const Cell
         const double db = lerp(dba, dbb, d2);
         prim[p] = lerp(da, db, d3);
     }
+}
+
+__device__ __forceinline__ void trilinear8(const mk_snapshot_view &s, const CellPos &c, double prim[8]) {
+    trilinear8_impl<true>(s, c, prim);
+}
+__device__ __forceinline__ void trilinear8_fast(const mk_snapshot_view &s, const CellPos &c, double prim[8]) {
+    trilinear8_impl<false>(s, c, prim);
 }
 
 // fluid scalars at one point (athenak.py:759-794); k = photon wavevector

@@ -238,10 +238,10 @@ __device__ __forceinline__ void sample_fp64(const mk_request &R, const mk_snapsh
                                             double P[MK_MAX_NU], int &nsamples, double &max_tau, int64_t pix,
                                             int64_t row) {
     CellPos c;
-    if (!locate(sv, s[1], s[2], s[3], c)) return;
+    if (!locate_fast(sv, s[1], s[2], s[3], c)) return;
     ++nsamples;
     double prim[8];
-    trilinear8(sv, c, prim);
+    trilinear8_fast(sv, c, prim);
     const FluidFrame fs = fluid_frame_m(prim, m, s + 4, R.cos_fallback_pitch);
     // derived quantities (images.py:87-102)
     // quotients as products with rcp64 reciprocals (within a few ulp of the
