@@ -6,9 +6,10 @@ bhspin, fluid_gamma=None)`` with ``get_fluid_scalars_from_geodesics`` and
 GPU as ghost-filled AoS float32 meshblocks (built by ``mk_snapshot_build``);
 every sampling call runs in the sm_103a kernels.
 
-``grmhd_filename`` may be a path to an ``.athdf`` file (needs h5py) or a
-``SnapshotArrays`` (the synthetic generators' output, or arrays the caller
-read itself).  Single- and multi-level meshes: the ghost fill of
+``grmhd_filename`` may be a path to an ``.athdf`` file (read by this
+package's own HDF5 reader, ``grmhd/hdf5.py``; h5py is used only for files
+that reader refuses, when h5py is installed) or a ``SnapshotArrays`` (the
+synthetic generators' output, or arrays the caller read itself).  Single- and multi-level meshes: the ghost fill of
 athenak.py:67-525 runs on the device (``mk_snapshot_build``).
 """
 
@@ -25,16 +26,28 @@ from .grmhd import GRMHDFluidModel
 from .synthetic import SnapshotArrays, VARIABLE_NAMES
 
 
+_ATHDF_DATASETS = ("x1v", "x2v", "x3v", "x1f", "x2f", "x3f", "uov", "B", "LogicalLocations", "Levels")
+
+
 def load_athdf(path):
-    """Read the datasets load_athenak_meshblocks reads (athenak.py:77-97)."""
+    """Read the datasets load_athenak_meshblocks reads (athenak.py:77-97):
+    x1v..x3f, uov, B, LogicalLocations, Levels and the root attribute
+    VariableNames, with this package's HDF5 reader (no h5py); a file using
+    a part of HDF5 that reader does not implement is read with h5py when
+    it is installed, else the reader's error is raised."""
+    from .hdf5 import File, HDF5Error
     try:
-        import h5py
-    except ImportError as e:  # pragma: no cover - h5py is optional
-        raise RuntimeError("reading .athdf files needs h5py; pass a SnapshotArrays instead") from e
-    with h5py.File(path, "r") as f:
-        names = [n.decode("utf-8") for n in f.attrs["VariableNames"]]
-        d = {k: np.array(f[k]) for k in ("x1v", "x2v", "x3v", "x1f", "x2f", "x3f", "uov", "B",
-                                         "LogicalLocations", "Levels")}
+        f = File(path)
+        names = [bytes(n).split(b"\0")[0].decode("utf-8") for n in np.atleast_1d(f.attrs["VariableNames"])]
+        d = {k: f[k] for k in _ATHDF_DATASETS}
+    except HDF5Error:
+        try:
+            import h5py
+        except ImportError:
+            raise
+        with h5py.File(path, "r") as hf:
+            names = [n.decode("utf-8") for n in hf.attrs["VariableNames"]]
+            d = {k: np.array(hf[k]) for k in _ATHDF_DATASETS}
     return SnapshotArrays(uov=d["uov"].astype(np.float32), B=d["B"].astype(np.float32), x1v=d["x1v"],
                           x2v=d["x2v"], x3v=d["x3v"], x1f=d["x1f"], x2f=d["x2f"], x3f=d["x3f"],
                           LogicalLocations=d["LogicalLocations"], Levels=d["Levels"],

@@ -168,14 +168,7 @@ class Scheduler:
         The GPU is one server: batches on several slots share it."""
         if self.predict is None:
             return 0.0
-        left = 0.0
-        for busy in self.slots:
-            if busy is None:
-                continue
-            _, _, tickets = busy
-            work = sum(t.predicted for t in tickets)
-            left += max(0.0, tickets[0].launched + work - now)
-        return left + sum(t.predicted for t in self.pending)
+        return self._inflight_left(now) + sum(t.predicted for t in self.pending)
 
     def cancel(self, ticket):
         """Cancel a request that has not been launched yet."""
@@ -204,21 +197,35 @@ class Scheduler:
                 self.in_flight_bytes -= t.out_bytes
             self.slots[s] = None
 
+    def _inflight_left(self, now):
+        """Predicted seconds the batches already on the GPU still need."""
+        left = 0.0
+        for busy in self.slots:
+            if busy is None:
+                continue
+            _, _, tickets = busy
+            left += max(0.0, tickets[0].launched + sum(t.predicted for t in tickets) - now)
+        return left
+
     def _pack(self):
         """FIFO requests that fit one bucket, the request cap and the budget.
         With a latency bound, waiting requests that can no longer finish in
         time are shed first, and a request joins the batch only if the
-        batch's predicted time (the sum of its members' predictions: one
-        batch returns all its images together) keeps every member within
-        its bound."""
+        batch's predicted finish -- the in-flight batches' remaining work
+        (a persistent render holds the SMs until it ends, so a batch on
+        another slot waits for it) plus the sum of the batch members'
+        predictions (one batch returns all its images together) -- keeps
+        every member within its bound."""
         bound = self.latency_bound
         now = self.clock()
+        ahead = 0.0
         if bound is not None:
+            ahead = self._inflight_left(now)
             for t in list(self.pending):
-                if (now - t.arrival) + t.predicted > bound * t.predicted:
+                if (now - t.arrival) + ahead + t.predicted > bound * t.predicted:
                     self.pending.remove(t)
-                    self._shed(t, now, f"waited {1e3 * (now - t.arrival):.1f} ms, cannot finish within "
-                                       f"{bound:g} x {1e3 * t.predicted:.1f} ms")
+                    self._shed(t, now, f"waited {1e3 * (now - t.arrival):.1f} ms with {1e3 * ahead:.1f} ms of "
+                                       f"work ahead, cannot finish within {bound:g} x {1e3 * t.predicted:.1f} ms")
         cap = max(self.ex.buckets)
         batch, rays, nbytes, work = [], 0, 0, 0.0
         free = self.free_bytes
@@ -228,7 +235,7 @@ class Scheduler:
             if nbytes + t.out_bytes > free:
                 break
             if bound is not None and batch:
-                w = work + t.predicted
+                w = ahead + work + t.predicted
                 if any((now - m.arrival) + w > bound * m.predicted for m in batch + [t]):
                     continue  # waits for a batch of its own
             batch.append(t)

@@ -148,3 +148,21 @@ def test_render_of_zero_rays_is_a_no_op(cuda, tiny_arrays):
                   ptr(prep.ws), prep.ws.numel() * 8, stream_ptr(None))
         torch.cuda.synchronize()
         assert bool((prep.images[0] == -7.0).all()), form
+
+
+def test_render_from_athdf_path_equals_arrays(cuda, tiny_arrays, tmp_path):
+    """AthenakFluidModel(path) -- the reference's call, the file read by the
+    package's own HDF5 reader -- renders the image the same arrays give,
+    bit for bit, in FP64 and in the mixed form."""
+    from mahakala_gb300.grmhd.athenak import AthenakFluidModel
+    from mahakala_gb300.grmhd.hdf5 import write_athdf
+    from mahakala_gb300.images import make_image
+    path = str(tmp_path / "tiny.athdf")
+    write_athdf(path, tiny_arrays, chunk_blocks=True, deflate=True)
+    from_file = AthenakFluidModel(path, tiny_arrays.bhspin, fluid_gamma=13. / 9)
+    from_arrays = AthenakFluidModel(tiny_arrays, tiny_arrays.bhspin, fluid_gamma=13. / 9)
+    kw = dict(camera_inclination=60, mass_scale=1e27, r_high=3, fov=30, resolution=16, max_nsteps=1500)
+    for form in ("fp64", "mixed"):
+        a = make_image(from_file, precision=form, **kw)
+        b = make_image(from_arrays, precision=form, **kw)
+        assert b.max() > 0 and np.array_equal(a, b), form

@@ -238,3 +238,22 @@ def test_latency_bound_needs_a_predictor():
         Scheduler(FakeExecutor(clock), hbm_budget=10 ** 9, clock=clock, latency_bound=2.0)
     with pytest.raises(ValueError):
         Scheduler(FakeExecutor(clock), hbm_budget=10 ** 9, clock=clock, latency_bound=1.0, predict=lambda r: 1.0)
+
+
+def test_latency_bound_counts_work_already_on_the_gpu():
+    """A persistent render holds the SMs until it ends, so a request is not
+    sent to a free slot beside a long batch when that batch's remaining work
+    would break the request's bound: with two free slots, a 900 ms request
+    and a 16 ms one submitted together, the long one launches and the short
+    one is shed instead of launching beside it."""
+    clock = Clock()
+    ex = FakeExecutor(clock, nslots=2, buckets=(100, 400, 1600), cost=1e-3)
+    s = Scheduler(ex, hbm_budget=10 ** 9, clock=clock, latency_bound=2.0,
+                  predict=lambda r: 1e-3 * int(r.resolution) ** 2)
+    big = s.submit(req(30))
+    small = s.submit(req(4))
+    s.step()
+    assert [x[2] for x in ex.launches] == [[big.id]]
+    assert small.status == "shed" and "work ahead" in small.error
+    drive(s, clock)
+    assert big.status == "done"
