@@ -387,7 +387,8 @@ def run_serving(torch, model0, n, precisions, latency_bound=2.0):
     second time with latency-bound admission (requests that cannot finish
     within latency_bound x their predicted isolated latency are shed; the
     predictor is each resolution's latency served alone, calibrated on
-    separate requests before the stream: the fastest of each resolution)."""
+    separate requests before the stream: the fastest and slowest of each
+    resolution)."""
     from mahakala_gb300 import configs
     from mahakala_gb300.grmhd.athenak import AthenakFluidModel
     from mahakala_gb300.serving import (DeviceExecutor, Scheduler, isolated_latencies, isolated_times,
@@ -436,11 +437,13 @@ def run_serving(torch, model0, n, precisions, latency_bound=2.0):
         by_res = {}
         for r in cal:
             by_res.setdefault(int(r.resolution), []).append(r)
-        # the fastest calibration request of each resolution: a request's own
-        # isolated time varies with spin and view (up to ~5x for FP64 64^2
-        # renders, whose time is their longest ray's chain), and a predictor
-        # above it would let the stream stretch that request beyond the bound
-        table = {res: float(np.min(isolated_latencies(factory, rs))) for res, rs in by_res.items()}
+        # per resolution, the fastest and the slowest calibration request: a
+        # request's isolated time varies with spin and view (several-fold
+        # for FP64 64^2 renders, whose time is their longest ray's chain), so
+        # its own bound takes the low figure and the work it puts ahead of
+        # later requests the high one
+        cal_t = {res: isolated_latencies(factory, rs) for res, rs in by_res.items()}
+        table = {res: (float(np.min(v)), float(np.max(v))) for res, v in cal_t.items()}
         known = sorted(table)
 
         def predict(r):
@@ -448,7 +451,7 @@ def run_serving(torch, model0, n, precisions, latency_bound=2.0):
             if res in table:
                 return table[res]
             near = min(known, key=lambda k: abs(k - res))
-            return table[near] * (res / near) ** 2
+            return tuple(x * (res / near) ** 2 for x in table[near])
         bsched = factory(latency_bound=latency_bound, predict=predict)
         torch.cuda.synchronize()
         btickets, bwall = serve_stream(bsched, arrivals, reqs)
@@ -458,9 +461,10 @@ def run_serving(torch, model0, n, precisions, latency_bound=2.0):
             brep["isolated_ms_p99"] = 1e3 * float(np.percentile(served_iso, 99))
             brep["p99_over_isolated_p99"] = brep["p99_ms"] / brep["isolated_ms_p99"]
         brep["latency_bound"] = latency_bound
-        brep["predictor_ms"] = {str(k): 1e3 * v for k, v in sorted(table.items())}
-        brep["predictor"] = "per resolution, the fastest isolated latency of 16 calibration requests not in the stream"
-        pred = [predict(r) for r in reqs]
+        brep["predictor_ms"] = {str(k): [1e3 * v[0], 1e3 * v[1]] for k, v in sorted(table.items())}
+        brep["predictor"] = ("per resolution, the fastest (own bound) and slowest (work ahead of others) isolated "
+                             "latency of 16 calibration requests not in the stream")
+        pred = [predict(r)[0] for r in reqs]
         over = [t.latency / pred[i] for i, t in enumerate(btickets) if t.status == "done"]
         if over:
             brep["latency_over_predicted_p99"] = float(np.percentile(over, 99))

@@ -63,7 +63,8 @@ class Ticket:
     status: str = "waiting"    # waiting | running | done | failed | cancelled | shed
     error: str = None
     batch: int = None
-    predicted: float = None    # predicted latency served alone (s), with a latency bound
+    predicted: float = None    # predicted latency served alone (s): its bound is latency_bound x this
+    work: float = None         # predicted GPU time it puts ahead of later requests (s)
 
     @property
     def latency(self):
@@ -112,9 +113,13 @@ class Scheduler:
 
     def __init__(self, executor, hbm_budget, max_requests=MAX_REQUESTS_PER_BATCH, clock=time.perf_counter,
                  latency_bound=None, predict=None):
-        """latency_bound (k) with predict(request) -> seconds: shed requests
-        that cannot be served within k times their predicted isolated
-        latency (see the module docstring); None admits by budget only."""
+        """latency_bound (k) with predict(request) -> seconds, or -> (low,
+        high) seconds: shed requests that cannot be served within k times
+        their predicted isolated latency (see the module docstring); with a
+        pair, the low figure sets the request's own bound and the high one
+        the work it puts ahead of later requests (an isolated time that
+        varies from request to request then errs on the safe side both
+        ways).  None admits by budget only."""
         if (latency_bound is None) != (predict is None):
             raise ValueError("latency_bound and predict go together")
         if latency_bound is not None and not latency_bound > 1.0:
@@ -148,7 +153,9 @@ class Scheduler:
                    self.clock() if arrival is None else arrival)
         self.tickets.append(t)
         if self.latency_bound is not None:
-            t.predicted = float(self.predict(req))
+            p = self.predict(req)
+            lo, hi = (p, p) if np.ndim(p) == 0 else p
+            t.predicted, t.work = float(lo), float(max(lo, hi))
             now = self.clock()
             ahead = self.backlog(now)
             if (now - t.arrival) + ahead + t.predicted > self.latency_bound * t.predicted:
@@ -168,7 +175,7 @@ class Scheduler:
         The GPU is one server: batches on several slots share it."""
         if self.predict is None:
             return 0.0
-        return self._inflight_left(now) + sum(t.predicted for t in self.pending)
+        return self._inflight_left(now) + sum(t.work for t in self.pending)
 
     def cancel(self, ticket):
         """Cancel a request that has not been launched yet."""
@@ -204,7 +211,7 @@ class Scheduler:
             if busy is None:
                 continue
             _, _, tickets = busy
-            left += max(0.0, tickets[0].launched + sum(t.predicted for t in tickets) - now)
+            left += max(0.0, tickets[0].launched + sum(t.work for t in tickets) - now)
         return left
 
     def _pack(self):
@@ -235,13 +242,15 @@ class Scheduler:
             if nbytes + t.out_bytes > free:
                 break
             if bound is not None and batch:
-                w = ahead + work + t.predicted
-                if any((now - m.arrival) + w > bound * m.predicted for m in batch + [t]):
+                # member m finishes after the work ahead, the other members'
+                # work and its own time
+                w = ahead + work + t.work
+                if any((now - m.arrival) + w - m.work + m.predicted > bound * m.predicted for m in batch + [t]):
                     continue  # waits for a batch of its own
             batch.append(t)
             rays += t.rays
             nbytes += t.out_bytes
-            work += t.predicted or 0.0
+            work += t.work or 0.0
         return batch, rays
 
     def step(self):

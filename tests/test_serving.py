@@ -257,3 +257,21 @@ def test_latency_bound_counts_work_already_on_the_gpu():
     assert small.status == "shed" and "work ahead" in small.error
     drive(s, clock)
     assert big.status == "done"
+
+
+def test_latency_bound_uses_low_for_own_bound_and_high_for_work_ahead():
+    """With (low, high) predictions a request alone is admitted on its low
+    figure, while the work it puts ahead of a later request counts at its
+    high figure."""
+    clock = Clock()
+    ex = FakeExecutor(clock, nslots=2, buckets=(100, 400, 1600), cost=1e-3)
+    s = Scheduler(ex, hbm_budget=10 ** 9, clock=clock, latency_bound=2.0,
+                  predict=lambda r: (1e-3 * int(r.resolution) ** 2, 3e-3 * int(r.resolution) ** 2))
+    first = s.submit(req(10))          # low 0.1 s, high 0.3 s: alone, within 2 x 0.1
+    s.step()
+    assert first.status == "running"
+    clock.t = 0.15                     # by the low figure it is done; by the high one 0.15 s remain
+    later = s.submit(req(8), arrival=clock.t)   # low 0.064 s: 0.15 + 0.064 > 0.128
+    assert later.status == "shed"
+    drive(s, clock)
+    assert first.status == "done"
