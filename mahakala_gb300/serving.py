@@ -20,7 +20,9 @@ and a factor k, a request whose predicted latency in the stream (the
 predicted work queued ahead of it plus its own) exceeds k times its
 isolated latency is shed at submission, and a waiting request that can no
 longer finish within k times its isolated latency is shed before launch.
-Shed requests end with status "shed" (reported as failures), so under an
+A batch is also held back while launching it would delay a running
+request past its own bound (concurrent renders share the GPU).  Shed
+requests end with status "shed" (reported as failures), so under an
 offered load above what the GPU can serve the served requests keep their
 latency bound instead of the queue growing without end.  Latency is
 measured from arrival to the moment its image is in host memory.
@@ -214,6 +216,17 @@ class Scheduler:
             left += max(0.0, tickets[0].launched + sum(t.work for t in tickets) - now)
         return left
 
+    def _inflight_keep_bounds(self, batch, now):
+        """Concurrent renders share the GPU, so a new batch's work delays the
+        batches already running by up to that work: launch it only if every
+        running request still finishes within its bound, counting all the
+        in-flight work left plus the new batch's."""
+        running = [t for busy in self.slots if busy is not None for t in busy[2]]
+        if not running:
+            return True
+        delay = self._inflight_left(now) + sum(t.work for t in batch)
+        return all((now - t.arrival) + delay <= self.latency_bound * t.predicted for t in running)
+
     def _pack(self):
         """FIFO requests that fit one bucket, the request cap and the budget.
         With a latency bound, waiting requests that can no longer finish in
@@ -265,8 +278,10 @@ class Scheduler:
             batch, rays = self._pack()
             if not batch:
                 break
-            bucket = min(b for b in self.ex.buckets if b >= rays)
             now = self.clock()
+            if self.latency_bound is not None and not self._inflight_keep_bounds(batch, now):
+                break  # it waits: launching now would push a running request past its bound
+            bucket = min(b for b in self.ex.buckets if b >= rays)
             for t in batch:
                 self.pending.remove(t)
                 t.admitted = t.launched = now

@@ -275,3 +275,22 @@ def test_latency_bound_uses_low_for_own_bound_and_high_for_work_ahead():
     assert later.status == "shed"
     drive(s, clock)
     assert first.status == "done"
+
+
+def test_latency_bound_holds_back_a_batch_that_would_delay_a_running_request():
+    """A long request is not launched beside a running short one when the
+    shared GPU would push the short one past its bound; it launches once
+    the short one is done."""
+    clock = Clock()
+    ex = FakeExecutor(clock, nslots=2, buckets=(100, 400, 1600), cost=1e-3)
+    s = Scheduler(ex, hbm_budget=10 ** 9, clock=clock, latency_bound=2.0,
+                  predict=lambda r: 1e-3 * int(r.resolution) ** 2)
+    short = s.submit(req(10))          # 0.1 s
+    s.step()
+    clock.t = 0.01
+    long_ = s.submit(req(20))          # 0.4 s: 0.01 + 0.09 + 0.4 > 0.2 for the short one
+    s.step()
+    assert [x[2] for x in ex.launches] == [[short.id]] and long_.status == "waiting"
+    drive(s, clock)
+    assert short.status == "done" and long_.status == "done"
+    assert [x[2] for x in ex.launches] == [[short.id], [long_.id]]
