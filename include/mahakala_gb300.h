@@ -53,7 +53,13 @@ typedef enum {
    MK_MIXED_STRICT: as MK_MIXED, but near the hole the whole geodesic step
    (accelerations included) is binary64.
    MK_MIXED_DF: as MK_MIXED_STRICT with that step in double-float (pairs of
-   FP32, ~1e-13 relative) instead of binary64 -- not IEEE FP64. */
+   FP32, ~1e-13 relative) instead of binary64 -- not IEEE FP64.
+   The mixed forms end a ray that moves outward beyond the snapshot's
+   bounding radius with MK_RAY_ESCAPED: outside the photon region it has no
+   radial turning point left, takes no further sample and its intensity is
+   final, so the image equals running it on to the reference's stop; its
+   nsteps is the steps taken (mk_set_tuning "escape_cut" 0 runs every ray
+   to the reference's stop).  MK_FP64 always follows the reference's rule. */
 typedef enum { MK_FP64 = 0, MK_MIXED = 1, MK_MIXED_DF = 2, MK_MIXED_STRICT = 3 } mk_precision;
 
 typedef enum {
@@ -365,6 +371,8 @@ int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_ra
    compiled for 3 resident blocks per SM (no register spills), 4 (128
    registers) or 5 (96 registers); 0 takes 4 when the launch's rays fit one
    wave of 4-block slots and 5 otherwise.
+   "escape_cut" (0 or 1; default 1): the mixed forms end outbound rays
+   beyond the snapshot's bounding radius (see mk_precision).
    "phase_events" (0 or 1; default 0): renders record CUDA events on their
    stream around each kernel for mk_render_phase_ms; not for renders that
    are captured into a CUDA graph. */

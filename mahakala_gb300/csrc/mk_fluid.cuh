@@ -386,17 +386,24 @@ struct CellPosF {
     float del[3];
 };
 
+// r_out: a Kerr-Schild radius beyond which no point of the snapshot's block
+// grid lies (r <= |x| in these coordinates, so the largest corner distance
+// of the grid, rounded up by 1 M, bounds it)
 struct SnapF32 {
-    float lo[3], inv_w[3];
+    float lo[3], inv_w[3], r_out;
 };
 
 __device__ __forceinline__ SnapF32 snap_f32(const mk_snapshot_view &s) {
     SnapF32 f;
+    double rr = 0.0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         f.lo[a] = (float)s.lo[a];
         f.inv_w[a] = (float)(1.0 / s.width[a]);
+        const double e = fmax(fabs(s.lo[a]), fabs(s.lo[a] + s.nb[a] * s.width[a]));
+        rr += e * e;
     }
+    f.r_out = (float)(sqrt(rr) + 1.0);
     return f;
 }
 

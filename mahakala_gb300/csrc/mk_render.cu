@@ -58,7 +58,9 @@ constexpr double R_TURN = 6.0;
 // MK_MIXED_STRICT / MK_MIXED_DF; MK_MIXED's parked rays come from phase A's
 // float-pair state, null to well under half a float ulp of k^t (the images
 // were bit-identical with and without), and skip it
-enum : int { F32_HANDOFF = 1, F32_PARK = 2, F32_RENULL = 4 };
+// F32_ESCAPE (mixed forms): a ray moving outward beyond the snapshot's
+// bounding radius r_out ends there as escaped (see g_escape_cut).
+enum : int { F32_HANDOFF = 1, F32_PARK = 2, F32_RENULL = 4, F32_ESCAPE = 8 };
 
 // rays per warp in the mixed form's FP64 phase (mk_set_tuning
 // "fp64_rays_per_warp"): 32 fills every lane; fewer rays per warp shorten
@@ -73,6 +75,15 @@ static int g_fp64_zone = 1;
 // spills); 0 picks 4 when the launch's rays fit the GPU's 4-block slots in
 // one wave and 5 when they do not (more resident warps pay only then)
 static int g_f32_blocks = 0;
+// 1: the mixed forms end a ray moving outward beyond the snapshot's
+// bounding radius (SnapF32::r_out) with MK_RAY_ESCAPED.  Outside the photon
+// region a null geodesic has no radial turning point, so such a ray never
+// reaches the snapshot again: it takes no further sample and its intensity
+// is final -- the image is bit-identical to integrating on to the
+// reference's stop (r - r_EH > 1500), only its step count and the radius
+// it stops at differ.  The FP64 form always keeps the reference's rule.
+// 0: the mixed forms run every ray to the reference's stop as well.
+static int g_escape_cut = 1;
 // measurement switch: when set, each render records a CUDA event on its
 // stream before its first kernel and after each kernel, so the phases can
 // be timed apart (mk_render_phase_ms).  Process-wide, off by default; not
@@ -675,7 +686,7 @@ __device__ __forceinline__ void zone_barrier() {
 
 __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ reqs,
                                                const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws,
-                                               const RayRecord *q64, long long capacity, ZoneMsgs &msg) {
+                                               const RayRecord *q64, long long capacity, int escape, ZoneMsgs &msg) {
     const int lane = threadIdx.x & 31;
     unsigned long long *counter = &ws->q64_next;
     const long long total = min((long long)*(volatile unsigned long long *)&ws->q64_count, capacity);
@@ -804,6 +815,12 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                     msg.why[b][lane] = MK_RAY_MAXSTEPS;
                     msg.steps[b][lane] = steps;
                     active = false;
+                } else if (escape && !inzone && r_new > sf.r_out && dr > 0.0f) {
+                    // outbound beyond every snapshot cell: no sample follows
+                    flags |= ZM_END;
+                    msg.why[b][lane] = MK_RAY_ESCAPED;
+                    msg.steps[b][lane] = steps;
+                    active = false;
                 } else if (inzone && ((r_new >= (float)R_TURN && dr > 0.0f) ||
                                       (dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f))) {
                     // outbound past the photon-ring region, or a radial turning
@@ -893,14 +910,14 @@ __device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
 
 __global__ void __launch_bounds__(ZONE_THREADS)
 render_zone_kernel(const mk_request *__restrict__ reqs, const mk_snapshot_view *__restrict__ snaps,
-                   RenderWorkspace *ws, const RayRecord *q64, long long capacity) {
+                   RenderWorkspace *ws, const RayRecord *q64, long long capacity, int escape) {
     __shared__ ZoneMsgs msg;
     // warps 0 and 2 of a 4-warp block: 4-warp blocks spread the pairs over
     // the SMs' sub-partitions better than 2-warp blocks (measured ~5 %);
     // warps 1 and 3 leave at once
     const int w = threadIdx.x >> 5;
     if (w == 0)
-        zone_integrate(reqs, snaps, ws, q64, capacity, msg);
+        zone_integrate(reqs, snaps, ws, q64, capacity, escape, msg);
     else if (w == 2)
         zone_sample(reqs, snaps, ws, q64, msg);
 }
@@ -1060,7 +1077,11 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 if (steps >= R.policy.nmax - 1) {
                     finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_MAXSTEPS, nsamples, max_tau, ws);
                     active = false;
-                } else if (SRC == SRC_CAMERA && mode) {
+                } else if ((mode & F32_ESCAPE) && r_new > Q.sf.r_out && r_new > r_cur) {
+                    // outbound beyond every snapshot cell: no sample follows
+                    finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_ESCAPED, nsamples, max_tau, ws);
+                    active = false;
+                } else if (SRC == SRC_CAMERA && (mode & (F32_HANDOFF | F32_PARK))) {
                     // near the horizon or inbound in the photon-ring region: to
                     // the near-hole queue; outbound past it (F32_PARK): to the
                     // FP32 continuation queue, whose kernel runs beside the
@@ -1138,6 +1159,11 @@ extern "C" int mk_set_tuning(const char *name, int64_t value) {
         g_phase_events = (int)value;
         return MK_OK;
     }
+    if (!strcmp(name, "escape_cut")) {
+        MK_REQUIRE(value == 0 || value == 1, MK_ERR_ARG, "mk_set_tuning: escape_cut must be 0 or 1");
+        g_escape_cut = (int)value;
+        return MK_OK;
+    }
     if (!strcmp(name, "fp64_zone")) {
         MK_REQUIRE(value == 0 || value == 1, MK_ERR_ARG, "mk_set_tuning: fp64_zone must be 0 or 1");
         g_fp64_zone = (int)value;
@@ -1206,7 +1232,8 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
         f32_blocks = max_rays > (int64_t)device_sm_count() * 4 * RENDER_THREADS ? 5 : 4;
     // MK_MIXED parks the outbound rays: its FP32 continuation then runs beside
     // the near-hole phase instead of after it
-    const int mode = (g_fp64_zone ? F32_HANDOFF : 0) | (precision == MK_MIXED ? F32_PARK : 0);
+    const int mode = (g_fp64_zone ? F32_HANDOFF : 0) | (precision == MK_MIXED ? F32_PARK : 0) |
+                     (g_escape_cut ? F32_ESCAPE : 0);
     if (f32_blocks == 5)
         render_f32_kernel<SRC_CAMERA, 5>
             <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 5>, 5), max_rays), RENDER_THREADS, 0,
@@ -1225,7 +1252,7 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     // the device, so the grid is persistent.
     // MK_MIXED's FP32 queue holds parked phase-A rays; the other mixed forms'
     // hold the near-hole phase's exits
-    const int qmode = precision == MK_MIXED ? 0 : F32_RENULL;
+    const int qmode = (precision == MK_MIXED ? 0 : F32_RENULL) | (g_escape_cut ? F32_ESCAPE : 0);
     auto launch_f32_queue = [&](cudaStream_t s) {
         if (f32_blocks == 5)
             render_f32_kernel<SRC_QUEUE, 5>
@@ -1253,7 +1280,7 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
         MK_CUDA(cudaEventRecord(side->fork, st));
         MK_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
         render_zone_kernel<<<(unsigned)device_sm_count() * 4, ZONE_THREADS, 0, st>>>(reqs_dev, snaps_dev, ws, q64,
-                                                                                      cap);
+                                                                                      cap, g_escape_cut);
         MK_LAUNCHED("render_zone_kernel");
         launch_f32_queue(side->s);
         MK_LAUNCHED("render_f32_kernel (queue)");

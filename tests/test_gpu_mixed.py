@@ -216,3 +216,30 @@ def test_camera_states_precomputed_equal_inline(cuda, medium_model):
     a, b = full.images[0].cpu().numpy(), small.images[0].cpu().numpy()
     assert a.max() > 0
     assert np.array_equal(a, b, equal_nan=True)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_strict", "mixed_df"])
+def test_escape_cut_leaves_images_bit_identical(cuda, medium_model, precision):
+    """Ending outbound rays at the snapshot's bounding radius (the default)
+    against running them to the reference's stop: the same image bit for
+    bit, the same captured rays, fewer steps, and the cut rays escaped."""
+    from mahakala_gb300 import _lib, configs
+    from mahakala_gb300.images import PreparedRender, RenderRequest
+    kw = dict(camera_inclination=60.0, resolution=32, fov=50.0, max_nsteps=8192,
+              mass_scale=configs.stable_mass_scale(40, 60.0, 86e9), observing_frequency=[86e9, 230e9])
+    cut = PreparedRender([RenderRequest(medium_model, **kw)], precision=precision, with_steps=True)
+    cut.launch()
+    _lib.call("mk_set_tuning", b"escape_cut", 0)
+    try:
+        full = PreparedRender([RenderRequest(medium_model, **kw)], precision=precision, with_steps=True)
+        full.launch()
+    finally:
+        _lib.call("mk_set_tuning", b"escape_cut", 1)
+    a, b = cut.images[0].cpu().numpy(), full.images[0].cpu().numpy()
+    assert np.all(np.isfinite(b)) and b.max() > 0 and np.array_equal(a, b)
+    sa, sb = (x.requests[0].out["status"].cpu().numpy() for x in (cut, full))
+    na, nb = (x.requests[0].out["nsteps"].cpu().numpy() for x in (cut, full))
+    assert np.array_equal(sa == _lib.MK_RAY_CAPTURED, sb == _lib.MK_RAY_CAPTURED)
+    moved = na != nb
+    assert moved.any() and np.all(na[moved] < nb[moved]) and np.all(sa[moved] == _lib.MK_RAY_ESCAPED)
+    assert cut.work_totals()[0] < full.work_totals()[0]
