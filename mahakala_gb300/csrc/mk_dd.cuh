@@ -76,10 +76,26 @@ __host__ __device__ __forceinline__ dd inv_sqrt(dd x) {
     return yy + yy * e * dd(0.5f, 0.0f);
 }
 
+// Float unit approximations (PTX rsqrt.approx.ftz / rcp.approx.ftz, ~2 ulp)
+// with subnormal inputs and results flushed to zero: the float geodesic's
+// arguments (r^2, Q ~ r^4, (r^4 + a^2 z^2)(r^2 + a^2), the step rule's
+// divisor) and the emission's are normal numbers, or give a zero emission
+// either way, so the flush changes nothing and saves the subnormal handling.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // ------------------------------------------------------------------------
 // Binary64 reciprocal square root and reciprocal for the FP64 path, whose
 // time is its FP64-pipe instruction count (1/64 of the FP32 rate on this
-// part).  The seed is the float unit's approximation (rsqrtf, __fdividef)
+// part).  The seed is the float unit's approximation (rsqrt_ftz, rcp_ftz)
 // of the argument moved to float and back by bit operations on the integer
 // pipe -- exponent rebased between the two formats, significand truncated
 // to 23 bits -- so only the correction runs on the FP64 pipe.  One
@@ -112,7 +128,7 @@ __device__ __forceinline__ bool f64_seed_range(unsigned hi) { return (hi >> 20) 
 
 __device__ __forceinline__ double rsqrt64(double x) {
     if (f64_seed_range((unsigned)((unsigned long long)__double_as_longlong(x) >> 32))) {
-        const double y = f64_bits_of(rsqrtf(f32_bits_of(x)));
+        const double y = f64_bits_of(rsqrt_ftz(f32_bits_of(x)));
         const double e = fma(-(x * y), y, 1.0);          // 1 - x y^2
         return fma(y * e, fma(0.375, e, 0.5), y);        // y (1 + e/2 + 3e^2/8)
     }
@@ -130,7 +146,7 @@ __device__ __forceinline__ double rcp64(double d) {
     const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(d) >> 32);
     if (f64_seed_range(hi & 0x7fffffffu)) {
         const double a = __hiloint2double((int)(hi & 0x7fffffffu), __double2loint(d));  // |d|
-        const double y = f64_bits_of(__fdividef(1.0f, f32_bits_of(a)), hi & 0x80000000u);
+        const double y = f64_bits_of(rcp_ftz(f32_bits_of(a)), hi & 0x80000000u);
         const double e = fma(-d, y, 1.0);                  // 1 - d y
         return fma(y, fma(e, e, e), y);                    // y (1 + e + e^2)
     }

@@ -504,21 +504,21 @@ struct FluidF32 {
 // ~1e-7 and ~1e-6; sqrt(0) = 0, cbrt(0) = 0, NaN and inf propagate).
 __device__ __forceinline__ float sqrt_approx(float x) {
     float r;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
 __device__ __forceinline__ float cbrt_approx(float x) {
     float l, r;
-    asm("lg2.approx.f32 %0, %1;" : "=f"(l) : "f"(x));
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l) : "f"(x));
     l *= 0.333333343f;
-    asm("ex2.approx.f32 %0, %1;" : "=f"(r) : "f"(l));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(l));
     return r;
 }
 
 __device__ __forceinline__ FluidF32 fluid_frame_f32(const float prim[8], const KerrPoint<float> &m, const float k[4],
                                                     float cos_fallback) {
     const float f = m.f, l1 = m.l1, l2 = m.l2, l3 = m.l3;
-    const float alpha = rsqrtf(1.0f + f);
+    const float alpha = rsqrt_ftz(1.0f + f);
     const float U1 = prim[1], U2 = prim[2], U3 = prim[3];
     const float lU = l1 * U1 + l2 * U2 + l3 * U3;
     const float gamma = sqrt_approx(1.0f + ((U1 * U1 + U2 * U2 + U3 * U3) + f * lU * lU));
@@ -530,7 +530,7 @@ __device__ __forceinline__ FluidF32 fluid_frame_f32(const float prim[8], const K
     const float ud0 = -uc0 + flu, ud1 = uc1 + l1 * flu, ud2 = uc2 + l2 * flu, ud3 = uc3 + l3 * flu;
     const float B1 = prim[5], B2 = prim[6], B3 = prim[7];
     const float bc0 = B1 * ud1 + B2 * ud2 + B3 * ud3;
-    const float iuc0 = __fdividef(1.0f, uc0);
+    const float iuc0 = rcp_ftz(uc0);
     const float bc1 = (B1 + uc1 * bc0) * iuc0, bc2 = (B2 + uc2 * bc0) * iuc0, bc3 = (B3 + uc3 * bc0) * iuc0;
     const float lb = bc0 + l1 * bc1 + l2 * bc2 + l3 * bc3;
     const float flb = f * lb;
@@ -540,7 +540,7 @@ __device__ __forceinline__ FluidF32 fluid_frame_f32(const float prim[8], const K
     const float kdotb = k[0] * bd0 + k[1] * bd1 + k[2] * bd2 + k[3] * bd3;
     const float bdotb = bc0 * bd0 + bc1 * bd1 + bc2 * bd2 + bc3 * bd3;
     const float bmag = sqrt_approx(bdotb);
-    float cp = __fdividef(kdotb, fabsf(o.kdotu) * bmag);
+    float cp = fdiv(kdotb, fabsf(o.kdotu) * bmag);
     if (isnan(cp)) cp = cos_fallback;
     o.cos_pitch = fminf(fmaxf(cp, -1.0f), 1.0f);
     o.dens = prim[0];

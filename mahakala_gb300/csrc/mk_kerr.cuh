@@ -67,11 +67,10 @@ __host__ __device__ constexpr dd sixth<dd>() { return dd(0x1.555556p-3f, -0x1.55
 
 // Quotient for each arithmetic: pairs divide exactly; binary64 multiplies
 // by rcp64's reciprocal (within 2 ulp; the division subroutine costs the
-// FP64 pipe several times more); the float (mixed-form) paths take the
-// hardware reciprocal (__fdividef: ~2 ulp, two instructions instead of a
-// division subroutine; |y| stays far below 2^126 here -- the largest
-// divisor, (r^4 + a^2 z^2)(r^2 + a^2) at the camera, is ~1e18).
-__device__ __forceinline__ float fdiv(float x, float y) { return __fdividef(x, y); }
+// FP64 pipe several times more); the float (mixed-form) paths multiply by
+// the hardware reciprocal (rcp.approx.ftz: ~2 ulp, two instructions
+// instead of a division subroutine).
+__device__ __forceinline__ float fdiv(float x, float y) { return x * rcp_ftz(y); }
 __device__ __forceinline__ double fdiv(double x, double y) { return x * rcp64(y); }
 __device__ __forceinline__ dd fdiv(dd x, dd y) { return x / y; }
 
@@ -115,9 +114,9 @@ __device__ __forceinline__ void kerr_accel_f32(float x, float y, float z, float 
     const float zz = z * z;
     const float kk = 0.5f * (x * x + y * y + zz - aa);
     const float Q = kk * kk + aa * zz;
-    const float iq = inv_sqrt(Q);
+    const float iq = rsqrt_ftz(Q);
     const float rr = fmaf(Q, iq, kk);        // sqrt(kk^2 + a^2 z^2) + kk
-    const float ir = inv_sqrt(rr);
+    const float ir = rsqrt_ftz(rr);
     const float r = rr * ir;
     const float i2rq = 0.5f * ir * iq;       // 1 / (2 r q)
     const float den = rr * rr + aa * zz;

@@ -337,13 +337,13 @@ __device__ __forceinline__ void emission_f32_at(const mk_snapshot_view &sv, cons
     trilinear8_f32(sv, c, prim);
     const FluidF32 fs = fluid_frame_f32(prim, m, s + 4, rc.cos_fb);
     const float bsq = fs.b * fs.b;
-    // float quotients by the hardware reciprocal (__fdividef, ~2 ulp)
-    const float beta = __fdividef(fs.u * rc.gam1, bsq) * 2.0f;
-    const float sigma = __fdividef(bsq, fs.dens);
+    // float quotients by the hardware reciprocal (fdiv: ~2 ulp)
+    const float beta = fdiv(fs.u * rc.gam1, bsq) * 2.0f;
+    const float sigma = fdiv(bsq, fs.dens);
     const float b2 = beta * beta;
-    const float T_ratio = __fdividef(rc.r_high * b2 + rc.r_low, 1.0f + b2);
+    const float T_ratio = fdiv(rc.r_high * b2 + rc.r_low, 1.0f + b2);
     // Theta_e = (MP/ME) u gem1 gim1 / (dens (gim1 + gem1 T_ratio))
-    const float Th = __fdividef((float)(MP / ME) * fs.u * rc.gem1 * rc.gim1, fs.dens * (rc.gim1 + rc.gem1 * T_ratio));
+    const float Th = fdiv((float)(MP / ME) * fs.u * rc.gem1 * rc.gim1, fs.dens * (rc.gim1 + rc.gem1 * T_ratio));
     const float Ne = rc.Ne_unit * fs.dens;
     const float Bg = rc.B_unit * fs.b;
     const float sin_p = sqrt_approx((1.0f - fs.cos_pitch) * (1.0f + fs.cos_pitch));
@@ -356,14 +356,14 @@ __device__ __forceinline__ void emission_f32_at(const mk_snapshot_view &sv, cons
     for (int ch = 0; ch < MK_MAX_NU; ch++) {
         if (ch < rc.nnu) {
             const float nusp = nus * sc[ch].inv_nu;  // nus / nu_obs
-            const float X = __fdividef(nup, nusp);
+            const float X = fdiv(nup, nusp);
             const float x3 = cbrt_approx(X);
             const float term = sqrt_approx(X) + (float)C2_11_12 * sqrt_approx(x3);
             // emissivity / nu'^2 (invariant, rescaled): k_em folds
             // sqrt2 pi EE^2 / (3 CL) and nu_obs
-            float em = __fdividef(Ne * sc[ch].k_em * nusp * term * term, 2.0f * th2 * nup * nup) * __expf(-x3);
+            float em = fdiv(Ne * sc[ch].k_em * nusp * term * term, 2.0f * th2 * nup * nup) * __expf(-x3);
             if (X > 1.e12f || cut) em = 0.0f;
-            const float bx = __fdividef(sc[ch].k_bx * nup, Th);
+            const float bx = fdiv(sc[ch].k_bx * nup, Th);
             // expm1(bx) (series below 2e-3; at radio frequencies bx ~ 1e-9);
             // a branch, so the library expm1f is not evaluated beside it
             float bden;
@@ -372,7 +372,7 @@ __device__ __forceinline__ void emission_f32_at(const mk_snapshot_view &sv, cons
             else
                 bden = expm1f(bx);
             // alpha nu' = (em nu'^2) / B_nu * nu' with B_nu = k_bnu nu'^3 / bden
-            float ab = __fdividef(em * bden, sc[ch].k_bnu);
+            float ab = fdiv(em * bden, sc[ch].k_bnu);
             em_out[ch] = isnan(em) ? 0.0f : em;
             ab_out[ch] = isnan(ab) ? 0.0f : ab;
         }
