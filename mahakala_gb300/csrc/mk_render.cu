@@ -201,6 +201,52 @@ __device__ __forceinline__ bool ray_in_request(const mk_request *__restrict__ re
     return pix >= 0 && pix < request_pixels(reqs[rq].camera);
 }
 
+// integer square root (floor) of 0 <= i < 2^31
+__device__ __forceinline__ int isqrt_floor(int i) {
+    int q = (int)sqrtf((float)i);
+    while (q > 0 && q * q > i) --q;
+    while ((q + 1) * (q + 1) <= i) ++q;
+    return q;
+}
+
+// The j-th pixel of an n x n grid in centre-out order: square rings around
+// the image centre, innermost first (rays near the centre reach the
+// photon-ring region and the horizon and take the most steps, so fetching
+// them first starts the longest chains when the launch starts); returns the
+// pixel index ix * n + iy.  A bijection of [0, n^2).
+__device__ __forceinline__ int64_t center_out_pixel(int64_t j64, int n) {
+    const int j = (int)j64;
+    int k, lo, side, e;
+    if (n & 1) {
+        const int c = (n - 1) >> 1;
+        if (j == 0) return (int64_t)c * n + c;
+        k = (isqrt_floor(j) + 1) >> 1;
+        e = j - (2 * k - 1) * (2 * k - 1);
+        lo = c - k;
+        side = 2 * k + 1;
+    } else {
+        k = isqrt_floor(j) >> 1;
+        e = j - 4 * k * k;
+        lo = (n >> 1) - 1 - k;
+        side = 2 * k + 2;
+    }
+    const int hi = lo + side - 1, edge = side - 1;
+    int ix, iy;
+    if (e < edge) { ix = lo + e; iy = lo; }
+    else if (e < 2 * edge) { ix = hi; iy = lo + (e - edge); }
+    else if (e < 3 * edge) { ix = hi - (e - 2 * edge); iy = hi; }
+    else { ix = lo; iy = hi - (e - 3 * edge); }
+    return (int64_t)ix * n + iy;
+}
+
+// pixel of a request for its local fetch index: centre-out on grid cameras
+// (the FP64 form: 1-3 % faster at 256x256; the mixed form's camera phase
+// keeps pixel order, in which its parked rays' queue coheres better --
+// centre-out there made the 1024x1024 stress render 20.6 -> 21.4 ms)
+__device__ __forceinline__ int64_t fetch_pixel(const mk_camera &c, int64_t local) {
+    return c.kind == MK_CAMERA_GRID ? center_out_pixel(local, c.pixels) : local;
+}
+
 // warp-aggregated work fetch: returns this lane's item index, -1 when the
 // lane asked and the work is exhausted, -2 when the lane did not ask
 __device__ __forceinline__ long long fetch(bool want, unsigned long long *counter, long long total) {
@@ -502,9 +548,9 @@ render_fp64_kernel(const mk_request *__restrict__ reqs, int nreq, long long tota
         if (!lane_works) exhausted = true;
         if (idx >= 0 && (SRC != SRC_CAMERA || ray_in_request(reqs, nreq, idx))) {
             if (SRC == SRC_CAMERA) {
-                ray = idx;
-                rq = find_request(reqs, nreq, ray);
-                pix = ray - reqs[rq].ray_offset;
+                rq = find_request(reqs, nreq, idx);
+                pix = fetch_pixel(reqs[rq].camera, idx - reqs[rq].ray_offset);
+                ray = reqs[rq].ray_offset + pix;
                 double s64[8];
                 camera_ray(reqs[rq].camera, pix, s64);
 #pragma unroll
