@@ -54,9 +54,10 @@ L2_FLUSH_BYTES = 256 << 20
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # each mixed-form kernel (phases A, B, C) on the 256x256 workload, from one
-# `ncu --set full` capture of
-# `python bench.py --precision mixed --steps 2 --warmup 3 --quick --serving 0`
-NCU_TRAFFIC_RENDER256 = {"A": 107.70e6 + 3.69e6, "B": 76.72e6 + 1.75e6, "C": 113.28e6 + 3.73e6}
+# capture of `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,
+# gpu__time_duration.sum -k regex:render_ -s 9 -c 3` over
+# `python bench.py --precision mixed --steps 2 --warmup 3 --quick --serving 0 --sampling-rays 0`
+NCU_TRAFFIC_RENDER256 = {"A": 106.92e6 + 3.01e6, "B": 76.73e6 + 0.04e6, "C": 113.40e6 + 0.16e6}
 
 # FP64 FLOP (DFMA = 2) per point of the standalone sampling stage, from ncu's
 # DADD/DMUL/DFMA thread-instruction counters on fluid_scalars_kernel (64x64
