@@ -32,6 +32,8 @@ import numpy as np
 
 SIGNATURE = b"\x89HDF\r\n\x1a\n"
 UNDEF = 0xFFFFFFFFFFFFFFFF
+MAX_BLOCKS = 4096     # continuation blocks of one object header
+MAX_DEPTH = 64        # B-tree levels
 
 
 class HDF5Error(ValueError):
@@ -59,6 +61,8 @@ class _Reader:
         raise HDF5Error("no HDF5 signature")
 
     def u(self, at, n):
+        if at < 0 or at + n > len(self.b):
+            raise HDF5Error(f"read of {n} bytes at {at} outside the file ({len(self.b)} bytes)")
         return int.from_bytes(self.b[at:at + n], "little")
 
     def addr(self, at):
@@ -110,7 +114,11 @@ class _Reader:
             size0 = self.u(p, n)
             p += n
             blocks = [(p, size0, True)]
+            seen = 0
             while blocks:
+                seen += 1
+                if seen > MAX_BLOCKS:
+                    raise HDF5Error("object header continuation blocks do not end")
                 start, size, first = blocks.pop(0)
                 q = start if first else start + 4  # "OCHK"
                 end = start + size if first else start + size - 4
@@ -127,7 +135,11 @@ class _Reader:
             raise HDF5Error(f"object header version {self.b[at]} not supported")
         nmsg = self.u(at + 2, 2)
         blocks = [(at + 16, self.u(at + 8, 4))]
+        seen = 0
         while blocks and len(out) < nmsg:
+            seen += 1
+            if seen > MAX_BLOCKS:
+                raise HDF5Error("object header continuation blocks do not end")
             start, size = blocks.pop(0)
             q, end = start, start + size
             while q + 8 <= end:
@@ -165,10 +177,14 @@ class _Reader:
         return self.absolute(self.addr(at + 8 + 2 * self.sl))
 
     def _cstr(self, at):
-        end = self.b.index(b"\0", at)
+        end = self.b.find(b"\0", at)
+        if at < 0 or end < 0:
+            raise HDF5Error("unterminated name in a local heap")
         return self.b[at:end].decode("utf-8")
 
-    def _btree_group(self, tree, heap, out):
+    def _btree_group(self, tree, heap, out, depth=0):
+        if depth > MAX_DEPTH:
+            raise HDF5Error("group B-tree deeper than the format allows")
         data = self._heap_data(heap)
         at = self.absolute(tree)
         if self.b[at:at + 4] != b"TREE" or self.b[at + 4] != 0:
@@ -178,7 +194,7 @@ class _Reader:
         for _ in range(used):
             child = self.addr(p)
             if level > 0:
-                self._btree_group(child, heap, out)
+                self._btree_group(child, heap, out, depth + 1)
             else:
                 self._snod(child, data, out)
             p += self.so + self.sl
@@ -255,6 +271,8 @@ class _Reader:
             raise HDF5Error("object is not a dataset")
         count = int(np.prod(shape, dtype=np.int64)) if shape else 1
         raw = self._layout_bytes(layout, dtype, shape, count, filters)
+        if len(raw) < count * dtype.itemsize:
+            raise HDF5Error(f"dataset data truncated ({len(raw)} of {count * dtype.itemsize} bytes)")
         arr = np.frombuffer(raw, dtype=dtype, count=count).reshape(shape)
         return arr.astype(dtype.newbyteorder("=")) if dtype.kind in "iuf" else arr.copy()
 
@@ -327,7 +345,9 @@ class _Reader:
             return out.tobytes()
         raise HDF5Error(f"layout class {cls} of layout version {ver} not supported")
 
-    def _btree_chunks(self, tree, ndim, cdims, out, filters, dtype):
+    def _btree_chunks(self, tree, ndim, cdims, out, filters, dtype, depth=0):
+        if depth > MAX_DEPTH:
+            raise HDF5Error("chunk B-tree deeper than the format allows")
         at = self.absolute(tree)
         if self.b[at:at + 4] != b"TREE" or self.b[at + 4] != 1:
             raise HDF5Error("bad chunk B-tree")
@@ -339,7 +359,7 @@ class _Reader:
             offs = [self.u(p + 8 + 8 * i, 8) for i in range(ndim)]
             child = self.addr(p + ksize)
             if level > 0:
-                self._btree_chunks(child, ndim, cdims, out, filters, dtype)
+                self._btree_chunks(child, ndim, cdims, out, filters, dtype, depth + 1)
             else:
                 a = self.absolute(child)
                 raw = self._unfilter(self.b[a:a + csize], filters, mask, dtype.itemsize)
@@ -369,11 +389,26 @@ class _Reader:
         return out
 
 
+def _decoding(fn):
+    """Raise HDF5Error for any failure to decode the file (a truncated or
+    damaged file surfaces as an index, value, struct or zlib error)."""
+    def wrapped(*args, **kwargs):
+        try:
+            return fn(*args, **kwargs)
+        except HDF5Error:
+            raise
+        except (IndexError, ValueError, struct.error, zlib.error, UnicodeDecodeError, RecursionError) as e:
+            raise HDF5Error(f"cannot decode the file: {e}") from e
+    wrapped.__name__, wrapped.__doc__ = fn.__name__, fn.__doc__
+    return wrapped
+
+
 class File:
     """A read-only HDF5 file: ``f[name]`` reads a dataset of the root group
     (NumPy array), ``f.attrs`` holds the root group's attributes, ``f.keys()``
     lists the root group's members."""
 
+    @_decoding
     def __init__(self, path):
         with open(path, "rb") as fh:
             self._r = _Reader(fh.read())
@@ -389,8 +424,13 @@ class File:
     def __getitem__(self, name):
         if name not in self._members:
             raise KeyError(name)
+        return self._dataset(name)
+
+    @_decoding
+    def _dataset(self, name):
         return self._r.dataset(self._members[name])
 
+    @_decoding
     def dataset_attrs(self, name):
         return self._r.attributes(self._members[name])
 

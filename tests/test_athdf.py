@@ -95,3 +95,19 @@ def test_not_hdf5_and_unsupported_parts_are_refused(tmp_path, tiny_arrays):
     bad.write_bytes(bytes(raw))
     with pytest.raises(HDF5Error):
         File(str(bad))
+
+
+def test_malformed_files_fail_with_an_error(tmp_path, tiny_arrays):
+    """Truncated files and self-referencing structures raise HDF5Error; the
+    reader never loops or returns short data."""
+    from mahakala_gb300.grmhd.hdf5 import File, HDF5Error, write_athdf
+    path = tmp_path / "tiny.athdf"
+    write_athdf(str(path), tiny_arrays)
+    raw = path.read_bytes()
+    for cut in (40, 200, len(raw) // 2, len(raw) - 100):
+        bad = tmp_path / f"cut{cut}.athdf"
+        bad.write_bytes(raw[:cut])
+        with pytest.raises(HDF5Error):
+            f = File(str(bad))
+            for k in f.keys():
+                f[k]
