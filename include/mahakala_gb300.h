@@ -32,7 +32,10 @@ typedef enum {
     MK_ERR_ARG = 1,          /* invalid argument (null pointer, bad size)   */
     MK_ERR_CUDA = 2,         /* a CUDA runtime call or launch failed        */
     MK_ERR_LIMIT = 3,        /* a size exceeds a documented maximum         */
-    MK_ERR_UNSUPPORTED = 4   /* valid request this build does not implement */
+    MK_ERR_UNSUPPORTED = 4,  /* valid request this build does not implement */
+    MK_ERR_TIMEOUT = 5       /* a bounded wait inside a kernel ran out: the
+                                launch's outputs are invalid (reported in the
+                                workspace header word MK_WS_ERROR)          */
 } mk_status;
 
 /* per-ray stop reasons (status arrays) */
@@ -290,7 +293,11 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
    the near-hole phase (MK_MIXED; its serial chain), MK_WS_STEPS_B /
    MK_WS_SAMPLES_B the steps and samples MK_MIXED's near-hole kernel took
    (near the hole and after), MK_WS_STEPS_C / MK_WS_SAMPLES_C those the
-   FP32 continuation kernel took (mixed forms). */
+   FP32 continuation kernel took (mixed forms), MK_WS_ERROR the waits of
+   MK_MIXED's near-hole pipeline that ran out (each bounded by the
+   "zone_wait_ns" tuning): nonzero means the launch's images are invalid,
+   and a host reads it as status MK_ERR_TIMEOUT once the stream has passed
+   the launch. */
 #define MK_WS_STEPS 1
 #define MK_WS_SAMPLES 2
 #define MK_WS_MAX_TAU 3
@@ -308,6 +315,7 @@ int mk_attenuated_emissivity(const double *em_dev, const double *ab_dev, const d
 #define MK_WS_SAMPLES_B 13
 #define MK_WS_STEPS_C 15
 #define MK_WS_SAMPLES_C 16
+#define MK_WS_ERROR 17
 size_t mk_render_workspace_bytes(int64_t total_rays, int32_t precision);
 
 /* make_image (images.py:30-144) for nreq requests in ONE persistent launch
@@ -375,7 +383,13 @@ int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_ra
    beyond the snapshot's bounding radius (see mk_precision).
    "phase_events" (0 or 1; default 0): renders record CUDA events on their
    stream around each kernel for mk_render_phase_ms; not for renders that
-   are captured into a CUDA graph. */
+   are captured into a CUDA graph.
+   "zone_wait_ns" (1 .. 6e10; default 1e9): the limit of each wait between
+   the warps of MK_MIXED's near-hole pipeline; a wait that runs out ends
+   its block and counts in the workspace word MK_WS_ERROR.
+   "zone_wait_test" (0 or 1; default 0): test switch -- the near-hole
+   pipeline's integrating warps withhold their first message, so the
+   launch ends through its wait limit and reports MK_WS_ERROR. */
 int mk_set_tuning(const char *name, int64_t value);
 
 /* Durations (ms) of the kernels of the last render launched with the

@@ -18,7 +18,7 @@ _I64 = _c.c_int64
 _D = _c.c_double
 _SZ = _c.c_size_t
 
-MK_OK, MK_ERR_ARG, MK_ERR_CUDA, MK_ERR_LIMIT, MK_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
+MK_OK, MK_ERR_ARG, MK_ERR_CUDA, MK_ERR_LIMIT, MK_ERR_UNSUPPORTED, MK_ERR_TIMEOUT = 0, 1, 2, 3, 4, 5
 MK_RAY_ACTIVE, MK_RAY_CAPTURED, MK_RAY_ESCAPED, MK_RAY_MAXSTEPS, MK_RAY_NAN = 0, 1, 2, 3, 4
 MK_FP64, MK_MIXED, MK_MIXED_DF, MK_MIXED_STRICT = 0, 1, 2, 3
 MK_POLICY_REFERENCE, MK_POLICY_FIXED = 0, 1
@@ -34,6 +34,7 @@ MK_WS_SAMPLES_FP64 = 10
 MK_WS_ZONE_RUN_MAX = 11
 MK_WS_STEPS_B, MK_WS_SAMPLES_B = 12, 13
 MK_WS_STEPS_C, MK_WS_SAMPLES_C = 15, 16
+MK_WS_ERROR = 17
 MK_MAX_REQUESTS_MIXED = 128
 
 

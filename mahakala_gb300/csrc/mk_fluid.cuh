@@ -407,22 +407,22 @@ __device__ __forceinline__ SnapF32 snap_f32(const mk_snapshot_view &s) {
     return f;
 }
 
-__device__ __forceinline__ bool locate_f32(const mk_snapshot_view &s, const SnapF32 &sf, float x, float y, float z,
-                                           CellPosF &c) {
-    const float xs[3] = {x, y, z};
+// index of the lookup-table cell holding (x, y, z), or -1 outside the grid
+__device__ __forceinline__ int64_t table_cell_f32(const mk_snapshot_view &s, const SnapF32 &sf, const float xs[3]) {
     int b[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const float u = (xs[a] - sf.lo[a]) * sf.inv_w[a];
-        if (!(u >= 0.0f && u < (float)s.nb[a])) return false;
+        if (!(u >= 0.0f && u < (float)s.nb[a])) return -1;
         b[a] = min((int)u, s.nb[a] - 1);
     }
-    const int mb = __ldg(s.table + ((int64_t)b[2] * s.nb[1] + b[1]) * s.nb[0] + b[0]);
-    if (mb < 0) return false;
-    c.mb = mb;
-    const float4 g0 = __ldg(reinterpret_cast<const float4 *>(s.geom_f32) + 2 * (int64_t)mb);
-    const float4 g1 = __ldg(reinterpret_cast<const float4 *>(s.geom_f32) + 2 * (int64_t)mb + 1);
-    const float left[3] = {g0.x, g0.y, g0.z}, inv_dx[3] = {g0.w, g1.x, g1.y};
+    return ((int64_t)b[2] * s.nb[1] + b[1]) * s.nb[0] + b[0];
+}
+
+// cell and offsets of (x, y, z) in a block with first cell centre `left`
+// and reciprocal cell widths inv_dx
+__device__ __forceinline__ void cell_in_block_f32(const mk_snapshot_view &s, const float xs[3], const float left[3],
+                                                  const float inv_dx[3], CellPosF &c) {
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const float t = (xs[a] - left[a]) * inv_dx[a] + 1.0f;  // ghost-shifted
@@ -434,6 +434,57 @@ __device__ __forceinline__ bool locate_f32(const mk_snapshot_view &s, const Snap
         c.idx[a] = i;
         c.del[a] = d;
     }
+}
+
+__device__ __forceinline__ bool locate_f32(const mk_snapshot_view &s, const SnapF32 &sf, float x, float y, float z,
+                                           CellPosF &c) {
+    const float xs[3] = {x, y, z};
+    const int64_t cell = table_cell_f32(s, sf, xs);
+    if (cell < 0) return false;
+    const int mb = __ldg(s.table + cell);
+    if (mb < 0) return false;
+    c.mb = mb;
+    const float4 g0 = __ldg(reinterpret_cast<const float4 *>(s.geom_f32) + 2 * (int64_t)mb);
+    const float4 g1 = __ldg(reinterpret_cast<const float4 *>(s.geom_f32) + 2 * (int64_t)mb + 1);
+    const float left[3] = {g0.x, g0.y, g0.z}, inv_dx[3] = {g0.w, g1.x, g1.y};
+    cell_in_block_f32(s, xs, left, inv_dx, c);
+    return true;
+}
+
+// The lookup-table cell, block and block geometry of a ray's last lookup,
+// kept in registers.  Consecutive steps of one ray mostly stay in one
+// table cell, and then locate_f32_cached finds the cell with no memory
+// access; locate_f32's two dependent loads (table, then geometry) sat on
+// the near-hole phase's serial chain at every step.  Reset it (key = -1)
+// whenever the ray or its snapshot changes.
+struct BlockCacheF {
+    int64_t key;
+    int mb;
+    float left[3], inv_dx[3];
+};
+
+__device__ __forceinline__ bool locate_f32_cached(const mk_snapshot_view &s, const SnapF32 &sf, float x, float y,
+                                                  float z, CellPosF &c, BlockCacheF &bc) {
+    const float xs[3] = {x, y, z};
+    const int64_t cell = table_cell_f32(s, sf, xs);
+    if (cell < 0) return false;
+    if (cell != bc.key) {
+        bc.key = cell;
+        bc.mb = __ldg(s.table + cell);
+        if (bc.mb >= 0) {
+            const float4 g0 = __ldg(reinterpret_cast<const float4 *>(s.geom_f32) + 2 * (int64_t)bc.mb);
+            const float4 g1 = __ldg(reinterpret_cast<const float4 *>(s.geom_f32) + 2 * (int64_t)bc.mb + 1);
+            bc.left[0] = g0.x;
+            bc.left[1] = g0.y;
+            bc.left[2] = g0.z;
+            bc.inv_dx[0] = g0.w;
+            bc.inv_dx[1] = g1.x;
+            bc.inv_dx[2] = g1.y;
+        }
+    }
+    if (bc.mb < 0) return false;
+    c.mb = bc.mb;
+    cell_in_block_f32(s, xs, bc.left, bc.inv_dx, c);
     return true;
 }
 

@@ -84,6 +84,14 @@ static int g_f32_blocks = 0;
 // it stops at differ.  The FP64 form always keeps the reference's rule.
 // 0: the mixed forms run every ray to the reference's stop as well.
 static int g_escape_cut = 1;
+// limit of each wait in the near-hole phase's pipeline, in ns
+// (mk_set_tuning "zone_wait_ns"); a wait that runs out aborts the block and
+// counts in the workspace header's MK_WS_ERROR word
+static unsigned long long g_zone_wait_ns = 1000000000ull;
+// test switch (mk_set_tuning "zone_wait_test"): the integrating warps
+// withhold their first message, so the first wait of every block's first
+// sampler can only run out -- the path by which a stalled pipeline ends
+static int g_zone_wait_test = 0;
 // measurement switch: when set, each render records a CUDA event on its
 // stream before its first kernel and after each kernel, so the phases can
 // be timed apart (mk_render_phase_ms).  Process-wide, off by default; not
@@ -162,6 +170,7 @@ struct RenderWorkspace {
     unsigned long long zone_exits;    // rays that left the near-hole phase outward (back to FP32)
     unsigned long long steps_c;       // steps the FP32 continuation over the FP32 queue took
     unsigned long long samples_c;     // samples it took
+    unsigned long long zone_error;    // bounded waits of the near-hole phase that ran out (images invalid)
 };
 constexpr size_t WS_HEADER = 256;
 static_assert(sizeof(RenderWorkspace) <= WS_HEADER, "workspace header");
@@ -332,17 +341,34 @@ __device__ __forceinline__ void sample_fp64(const mk_request &R, const mk_snapsh
 
 // Rescale k^t so that g(k, k) = 0 at x, keeping the spatial wavevector:
 // g00 k0^2 + 2 g0i k^i k0 + gij k^i k^j = 0, the root nearest the current k0.
+// Binary64 throughout, with the reciprocal and roots of the FP64 render
+// (rcp64, rsqrt64, sqrt64: within 2 ulp of the correctly rounded forms)
+// in place of the division and square-root subroutines: those made one
+// renormalisation ~200 FP64-pipe instructions, ~9 k cycles of the
+// near-hole phase's serial chain each time a lane of its warp reached a
+// radial turning point.
 __device__ __forceinline__ void renull_fp64(double s[8], double a) {
-    const KerrPoint<double> m = kerr_point(s[1], s[2], s[3], a);
-    const double f = m.f;
-    const double lk = m.l1 * s[5] + m.l2 * s[6] + m.l3 * s[7];
+    const double x = s[1], y = s[2], z = s[3];
+    const double aa = a * a, zz = z * z;
+    const double kk = 0.5 * (x * x + y * y + zz - aa);
+    const double Q = kk * kk + aa * zz;
+    const double rr = sqrt64(Q) + kk;
+    const double ir = rsqrt64(rr);
+    const double r = rr * ir;
+    const double den = rr * rr + aa * zz, rra = rr + aa;
+    const double inv2 = rcp64(den * rra);          // 1 / (den (r^2 + a^2))
+    const double f = 2.0 * (rr * r * (rra * inv2));
+    const double ira = den * inv2;
+    const double l1 = (r * x + a * y) * ira, l2 = (r * y - a * x) * ira, l3 = z * ir;
+    const double lk = l1 * s[5] + l2 * s[6] + l3 * s[7];
     const double A = -1.0 + f;                      // g00
     const double B = 2.0 * f * lk;                  // 2 g0i k^i
     const double C = s[5] * s[5] + s[6] * s[6] + s[7] * s[7] + f * lk * lk;
     const double disc = B * B - 4.0 * A * C;
     if (!(disc >= 0.0) || A == 0.0) return;
-    const double sq = sqrt(disc);
-    const double r1 = (-B + sq) / (2.0 * A), r2 = (-B - sq) / (2.0 * A);
+    const double sq = sqrt64(disc);
+    const double i2A = rcp64(2.0 * A);
+    const double r1 = (sq - B) * i2A, r2 = -(B + sq) * i2A;
     s[4] = fabs(r1 - s[4]) < fabs(r2 - s[4]) ? r1 : r2;
 }
 
@@ -693,51 +719,142 @@ __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix,
 // R_TURN outward is counted as back in FP32 and continues here.
 //
 // Few rays reach this phase and its time is the serial chain of the
-// longest one, so each block runs two warps on two sub-partitions: warp 0
-// integrates 32 rays while warp 1 takes the samples of their previous step
-// (emission, sums, the image write), one step behind.  They exchange one
-// message per lane and step through a double buffer in shared memory and
-// meet at one named barrier per step (both warps execute it once per
-// iteration; the integrator's last message carries ZM_DONE and both leave
-// after that barrier).  No wait depends on another block.
+// longest one, so each block is a pipeline of four warps on the SM's four
+// sub-partitions.  Warp 0 integrates 32 rays and posts one message per step
+// (per lane: the state after the step, the metric there, the step size,
+// flags).  Warps 1-3 take the messages in turn -- message j goes to warp
+// 1 + j % 3 -- and each locates the sample's cell, interpolates the
+// primitives and evaluates the emission, then folds the sample into the
+// lane's transfer sums in message order.  One warp takes ~2.4 k cycles for
+// a sample and ~1.3 k for an integration step (GB300, one block alone), so
+// with three samplers the integrating warp no longer waits on the samples,
+// and the cell lookup is off its chain too.
+//
+// Messages pass through ZONE_SLOTS slots in shared memory, each with two
+// mbarriers: `full` (the integrator's 32 lanes arrive after writing the
+// slot) and `empty` (its sampler's 32 lanes arrive after reading it).  The
+// fold order is a counter in shared memory: the sampler of message j folds
+// when it reads j and then sets it to j + 1.  Every wait is bounded
+// (mk_set_tuning "zone_wait_ns", 1 s by default): a wait that runs out sets
+// the block's abort flag and counts in the workspace header's MK_WS_ERROR
+// word, every warp of the block then leaves, and the launch's images are
+// invalid (the Python layer raises).  No wait depends on another block.
 enum : unsigned { ZM_START = 1u, ZM_SAMPLE = 2u, ZM_END = 4u, ZM_DONE = 16u, ZM_ZONE = 32u };
 constexpr int ZONE_THREADS = 128;
+constexpr int ZONE_SAMPLERS = 3;
+constexpr int ZONE_SLOTS = 6;  // a multiple of ZONE_SAMPLERS: each sampler alternates between two slots
+static_assert(ZONE_SLOTS % ZONE_SAMPLERS == 0 && ZONE_THREADS == 32 * (1 + ZONE_SAMPLERS), "zone pipeline");
 
-struct ZoneMsgs {
-    unsigned flags[2][32];
-    int idx[2][32];   // ZM_START: index in the near-hole queue
-    int steps[2][32];
-    int why[2][32];
-    float s[2][8][32];  // state after the step
-    float m[2][5][32];  // r, f, l1, l2, l3 there
-    float dt[2][32];    // the step's size
-    int cmb[2][32];     // located cell (mb = -1: outside the snapshot)
-    int cidx[2][3][32];
-    float cdel[2][3][32];
+struct ZoneSlot {
+    unsigned flags[32];
+    int idx[32];     // the lane's ray: its index in the near-hole queue
+    int steps[32];   // ZM_END: steps taken and stop reason
+    int why[32];
+    float s[7][32];  // ZM_SAMPLE: x^1..x^3, k^0..k^3 after the step
+    float m[5][32];  // r, f, l1, l2, l3 there
+    float dt[32];    // the step's size
 };
+
+struct ZoneShared {
+    ZoneSlot slot[ZONE_SLOTS];
+    // each lane's transfer sums, touched only by the sampler folding the
+    // lane's current message
+    float I[MK_MAX_NU][32], Ic[MK_MAX_NU][32], P[MK_MAX_NU][32];
+    float max_tau[32];
+    int nsamples[32];
+    unsigned long long full[ZONE_SLOTS], empty[ZONE_SLOTS];
+    int folded;  // messages folded so far
+    int abort;   // a wait of this block ran out
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+
+// release: this thread's earlier shared-memory writes are visible to a
+// thread whose wait on the phase succeeds
+__device__ __forceinline__ void mbar_arrive(unsigned long long *b) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(b))
+                 : "memory");
+}
+
+// acquire: true once the phase of parity `parity` has completed
+__device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait of a whole warp (every lane calls it and gets the same
+// answer) for the phase of parity `parity` of mbarrier b: false when
+// limit_ns ran out or the block aborted.
+__device__ __forceinline__ bool zone_wait(unsigned long long *b, unsigned parity, const ZoneShared &zs,
+                                          unsigned long long limit_ns) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned long long t0 = global_ns();
+    for (unsigned i = 1;; ++i) {
+        if (__all_sync(FULL, mbar_test(b, parity))) return true;
+        if ((i & 31u) == 0u) {
+            const bool stop = *(const volatile int *)&zs.abort != 0 || global_ns() - t0 > limit_ns;
+            if (__any_sync(FULL, stop)) return false;
+        }
+    }
+}
+
+// Bounded wait of a whole warp until `folded` reads j.
+__device__ __forceinline__ bool zone_wait_fold(const ZoneShared &zs, int j, unsigned long long limit_ns) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned long long t0 = global_ns();
+    for (unsigned i = 1;; ++i) {
+        if (__all_sync(FULL, *(const volatile int *)&zs.folded == j)) {
+            __threadfence_block();  // the sums written before `folded` was set
+            return true;
+        }
+        if ((i & 31u) == 0u) {
+            const bool stop = *(const volatile int *)&zs.abort != 0 || global_ns() - t0 > limit_ns;
+            if (__any_sync(FULL, stop)) return false;
+        }
+    }
+}
+
+// a wait ran out: stop the block's other warps and count it once per warp
+__device__ __forceinline__ void zone_fail(ZoneShared &zs, RenderWorkspace *ws) {
+    *(volatile int *)&zs.abort = 1;
+    if ((threadIdx.x & 31) == 0) atomicAdd(&ws->zone_error, 1ull);
+}
 
 // renull_fp64 on a float-pair state: only k^t changes
 __device__ __forceinline__ void renull_pair(const f2 X[4], f2 K[4], double a) {
     double s[8];
+    s[0] = 0.0;  // not read
 #pragma unroll
-    for (int i = 0; i < 4; i++) { s[i] = f2_to(X[i]); s[4 + i] = f2_to(K[i]); }
+    for (int i = 1; i < 4; i++) { s[i] = f2_to(X[i]); s[4 + i] = f2_to(K[i]); }
+    s[4] = (double)K[0].hi;  // only picks the nearer root
     renull_fp64(s, a);
     K[0] = f2_from(s[4]);
 }
 
-__device__ __forceinline__ void zone_barrier() {
-    __syncwarp();  // the warp arrives converged
-    asm volatile("bar.sync 1, 64;" ::: "memory");
-}
-
 __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ reqs,
                                                const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws,
-                                               const RayRecord *q64, long long capacity, int escape, ZoneMsgs &msg) {
+                                               const RayRecord *q64, long long capacity, int escape,
+                                               ZoneShared &zs, unsigned long long limit_ns, int withhold) {
     const int lane = threadIdx.x & 31;
     unsigned long long *counter = &ws->q64_next;
     const long long total = min((long long)*(volatile unsigned long long *)&ws->q64_count, capacity);
     bool active = false, exhausted = false;
-    int rq = 0, steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0, b_steps = 0;
+    int steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0, b_steps = 0, ray = -1;
     // float-pair state (X, K) throughout, as in the FP32 phases; near the
     // hole the wavevector is renormalised to null in binary64 on entry, at
     // every radial turning point and on the way out.  After the ray leaves
@@ -746,13 +863,17 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
     bool inzone = true;
     double bhspin = 0.0;
     f2 X[4], K[4];
-    mk_snapshot_view sv;  // this ray's snapshot, loaded once
     float xf[8];  // the state rounded to float
     float d1[4], dt = 0.0f, r_cur = 0.0f, dr_prev = 0.0f, reh = 0.0f, a = 0.0f, div = 0.0f, tol = 0.0f;
-    SnapF32 sf;
+    float r_out = 0.0f;
 
     for (int it = 0;; ++it) {
-        const int b = it & 1;
+        const int sl = it % ZONE_SLOTS;
+        ZoneSlot &msg = zs.slot[sl];
+        if (it >= ZONE_SLOTS && !zone_wait(&zs.empty[sl], (unsigned)((it / ZONE_SLOTS) - 1) & 1u, zs, limit_ns)) {
+            zone_fail(zs, ws);
+            return;
+        }
         unsigned flags = 0;
         const long long idx = fetch(!active && !exhausted, counter, total);
         if (idx == -1) exhausted = true;
@@ -762,8 +883,8 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
 #pragma unroll
             for (int i = 0; i < 8; i++) s[i] = q.s[i];
             steps = q.steps;
-            rq = q.rq;
-            const mk_request &R = reqs[rq];
+            ray = (int)idx;
+            const mk_request &R = reqs[q.rq];
             bhspin = R.camera.bhspin;
             nmax = R.policy.nmax;
             div = (float)R.policy.div;
@@ -771,8 +892,7 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             renull_fp64(s, bhspin);
             a = (float)bhspin;
             reh = (float)radius_eh(bhspin);
-            sv = snaps[R.snapshot];
-            sf = snap_f32(sv);
+            r_out = snap_f32(snaps[R.snapshot]).r_out;
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 X[i] = f2_from(s[i]);
@@ -787,13 +907,12 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             run = 0;
             inzone = true;
             flags |= ZM_START;
-            msg.idx[b][lane] = (int)idx;
             int why = MK_RAY_ACTIVE;
             dt = reference_dt(r_cur, reh, div, tol, why);
             if (dt == 0.0f || nmax < 2) {
                 flags |= ZM_END;
-                msg.why[b][lane] = why == MK_RAY_ACTIVE ? MK_RAY_MAXSTEPS : why;
-                msg.steps[b][lane] = steps;
+                msg.why[lane] = why == MK_RAY_ACTIVE ? MK_RAY_MAXSTEPS : why;
+                msg.steps[lane] = steps;
             } else {
                 active = true;
             }
@@ -813,9 +932,6 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                 xn[i] = Xn[i].hi;
                 xn[4 + i] = Kn[i].hi;
             }
-            CellPosF cell;
-            const bool inside = locate_f32(sv, sf, xn[1], xn[2], xn[3], cell);
-            if (inside) prefetch_cells_f32(sv, cell);
             KerrPoint<float> m;
             float dn[4];
             kerr_accel(xn[1], xn[2], xn[3], xn[4], xn[5], xn[6], xn[7], a, dn[0], dn[1], dn[2], dn[3], m);
@@ -825,8 +941,8 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             if (dtn == 0.0f) {
                 // the step is rejected and the ray stays frozen (geodesics.py:263-267)
                 flags |= ZM_END;
-                msg.why[b][lane] = w1;
-                msg.steps[b][lane] = steps;
+                msg.why[lane] = w1;
+                msg.steps[lane] = steps;
                 active = false;
             } else {
 #pragma unroll
@@ -837,16 +953,13 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                 for (int i = 0; i < 4; i++) d1[i] = dn[i];
                 flags |= ZM_SAMPLE | (inzone ? ZM_ZONE : 0u);
 #pragma unroll
-                for (int i = 0; i < 8; i++) msg.s[b][i][lane] = xn[i];
-                msg.m[b][0][lane] = m.r;
-                msg.m[b][1][lane] = m.f;
-                msg.m[b][2][lane] = m.l1;
-                msg.m[b][3][lane] = m.l2;
-                msg.m[b][4][lane] = m.l3;
-                msg.dt[b][lane] = dt;
-                msg.cmb[b][lane] = inside ? cell.mb : -1;
-#pragma unroll
-                for (int i = 0; i < 3; i++) { msg.cidx[b][i][lane] = cell.idx[i]; msg.cdel[b][i][lane] = cell.del[i]; }
+                for (int i = 0; i < 7; i++) msg.s[i][lane] = xn[1 + i];
+                msg.m[0][lane] = m.r;
+                msg.m[1][lane] = m.f;
+                msg.m[2][lane] = m.l1;
+                msg.m[3][lane] = m.l2;
+                msg.m[4][lane] = m.l3;
+                msg.dt[lane] = dt;
                 dt = dtn;
                 ++steps;
                 ++b_steps;
@@ -858,14 +971,14 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                 if (steps >= nmax - 1) {
                     // trajectory rows stop at N-1: step N-1 never reaches the solve
                     flags |= ZM_END;
-                    msg.why[b][lane] = MK_RAY_MAXSTEPS;
-                    msg.steps[b][lane] = steps;
+                    msg.why[lane] = MK_RAY_MAXSTEPS;
+                    msg.steps[lane] = steps;
                     active = false;
-                } else if (escape && !inzone && r_new > sf.r_out && dr > 0.0f) {
+                } else if (escape && !inzone && r_new > r_out && dr > 0.0f) {
                     // outbound beyond every snapshot cell: no sample follows
                     flags |= ZM_END;
-                    msg.why[b][lane] = MK_RAY_ESCAPED;
-                    msg.steps[b][lane] = steps;
+                    msg.why[lane] = MK_RAY_ESCAPED;
+                    msg.steps[lane] = steps;
                     active = false;
                 } else if (inzone && ((r_new >= (float)R_TURN && dr > 0.0f) ||
                                       (dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f))) {
@@ -884,71 +997,165 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                 dr_prev = dr;
             }
         }
-        msg.flags[b][lane] = flags | (any ? 0u : ZM_DONE);
-        zone_barrier();
-        if (!any) break;
+        msg.idx[lane] = ray;
+        msg.flags[lane] = flags | (any ? 0u : ZM_DONE);
+        __syncwarp();
+        if (!(withhold && it == 0)) mbar_arrive(&zs.full[sl]);
+        if (!any) {
+            // one ZM_DONE message for each of the other samplers
+            for (int e = 1; e < ZONE_SAMPLERS; ++e) {
+                const int jt = it + e, se = jt % ZONE_SLOTS;
+                if (jt >= ZONE_SLOTS &&
+                    !zone_wait(&zs.empty[se], (unsigned)((jt / ZONE_SLOTS) - 1) & 1u, zs, limit_ns)) {
+                    zone_fail(zs, ws);
+                    return;
+                }
+                zs.slot[se].flags[lane] = ZM_DONE;
+                zs.slot[se].idx[lane] = -1;
+                __syncwarp();
+                mbar_arrive(&zs.full[se]);
+            }
+            break;
+        }
     }
     if (zone_steps) atomicAdd(&ws->steps_fp64, (unsigned long long)zone_steps);
     if (b_steps) atomicAdd(&ws->steps_b, (unsigned long long)b_steps);
     if (run_max) atomicMax(&ws->zone_run_max, (unsigned long long)run_max);
 }
 
-__device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
+// Sampler k (warp 1 + k) of the pipeline: messages k, k + 3, k + 6, ...
+__device__ __forceinline__ void zone_sample(int k, const mk_request *__restrict__ reqs,
                                             const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws,
-                                            const RayRecord *q64, const ZoneMsgs &msg) {
+                                            const RayRecord *q64, ZoneShared &zs, unsigned long long limit_ns) {
+    const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    int rq = 0, nsamples = 0, zone_samples = 0, b_samples = 0;
+    int zone_samples = 0, b_samples = 0;
+    // constants of the ray this lane's last message belonged to
+    int cur = -1, rq = 0;
     int64_t pix = 0;
-    // Kahan-compensated float sums, as in phase A (binary64 sums cost this
-    // warp ~2.5 k cycles per sample on the chain's critical path)
-    float I[MK_MAX_NU], Ic[MK_MAX_NU], P[MK_MAX_NU], max_tau = 0.0f;
     SynchroF32 sc[MK_MAX_NU];
     RayF32 rc;
-    mk_snapshot_view sv;  // this ray's snapshot, loaded once
-    for (int it = 0;; ++it) {
-        const int b = it & 1;
-        zone_barrier();
-        const unsigned flags = msg.flags[b][lane];
-        if (flags & ZM_START) {
-            const RayRecord &q = q64[msg.idx[b][lane]];
+    mk_snapshot_view sv;
+    SnapF32 sf;
+    BlockCacheF bc;
+    bc.key = -1;
+    bc.mb = -1;
+    for (int j = k;; j += ZONE_SAMPLERS) {
+        const int sl = j % ZONE_SLOTS;
+        const ZoneSlot &msg = zs.slot[sl];
+        if (!zone_wait(&zs.full[sl], (unsigned)(j / ZONE_SLOTS) & 1u, zs, limit_ns)) {
+            zone_fail(zs, ws);
+            return;
+        }
+        const unsigned flags = msg.flags[lane];
+        const int idx = msg.idx[lane];
+        float x[8], dt = 0.0f;
+        KerrPoint<float> m;
+        int steps = 0, why = 0;
+        if (flags & ZM_SAMPLE) {
+            x[0] = 0.0f;  // x^0 is not read
 #pragma unroll
-            for (int ch = 0; ch < MK_MAX_NU; ch++) {
-                I[ch] = (float)q.I[ch];
-                Ic[ch] = (float)((double)I[ch] - q.I[ch]);
-                P[ch] = (float)q.P[ch];
-            }
-            max_tau = (float)q.max_tau;
-            nsamples = q.nsamples;
+            for (int i = 0; i < 7; i++) x[1 + i] = msg.s[i][lane];
+            m.r = msg.m[0][lane];
+            m.f = msg.m[1][lane];
+            m.l1 = msg.m[2][lane];
+            m.l2 = msg.m[3][lane];
+            m.l3 = msg.m[4][lane];
+            dt = msg.dt[lane];
+        }
+        if (flags & ZM_END) {
+            steps = msg.steps[lane];
+            why = msg.why[lane];
+        }
+        __syncwarp();
+        mbar_arrive(&zs.empty[sl]);  // the slot is free for message j + ZONE_SLOTS
+        if ((flags & (ZM_START | ZM_SAMPLE | ZM_END)) && idx != cur) {
+            cur = idx;
+            const RayRecord &q = q64[idx];
             rq = q.rq;
             const mk_request &R = reqs[rq];
             pix = q.ray - R.ray_offset;
             rc = ray_f32(R);
             sv = snaps[R.snapshot];
+            sf = snap_f32(sv);
+            bc.key = -1;
 #pragma unroll
             for (int ch = 0; ch < MK_MAX_NU; ch++)
                 if (ch < R.nnu) sc[ch] = synchro_consts(R.nu[ch]);
         }
-        if ((flags & ZM_SAMPLE) && msg.cmb[b][lane] >= 0) {
+        // the sample itself depends on no other message
+        float em[MK_MAX_NU], ab[MK_MAX_NU];
+        bool sampled = false;
+        if (flags & ZM_SAMPLE) {
             CellPosF c;
-            c.mb = msg.cmb[b][lane];
+            if (locate_f32_cached(sv, sf, x[1], x[2], x[3], c, bc)) {
+                emission_f32_at(sv, c, rc, x, m, sc, em, ab);
+                sampled = true;
+            }
+        }
+        float I0[MK_MAX_NU], Ic0[MK_MAX_NU], P0[MK_MAX_NU], tau0 = 0.0f;
+        int n0 = 0;
+        if (flags & ZM_START) {
+            // the sums the ray arrived with (read before waiting for the fold)
+            const RayRecord &q = q64[idx];
 #pragma unroll
-            for (int i = 0; i < 3; i++) { c.idx[i] = msg.cidx[b][i][lane]; c.del[i] = msg.cdel[b][i][lane]; }
-            float x[8];
+            for (int ch = 0; ch < MK_MAX_NU; ch++) {
+                I0[ch] = (float)q.I[ch];
+                Ic0[ch] = (float)((double)I0[ch] - q.I[ch]);
+                P0[ch] = (float)q.P[ch];
+            }
+            tau0 = (float)q.max_tau;
+            n0 = q.nsamples;
+        }
+        // fold in message order
+        if (!zone_wait_fold(zs, j, limit_ns)) {
+            zone_fail(zs, ws);
+            return;
+        }
+        if (flags & ZM_START) {
 #pragma unroll
-            for (int i = 0; i < 8; i++) x[i] = msg.s[b][i][lane];
-            KerrPoint<float> m;
-            m.r = msg.m[b][0][lane];
-            m.f = msg.m[b][1][lane];
-            m.l1 = msg.m[b][2][lane];
-            m.l2 = msg.m[b][3][lane];
-            m.l3 = msg.m[b][4][lane];
-            sample_f32(sv, c, rc, x, m, msg.dt[b][lane], I, Ic, P, sc, nsamples, max_tau);
+            for (int ch = 0; ch < MK_MAX_NU; ch++) {
+                zs.I[ch][lane] = I0[ch];
+                zs.Ic[ch][lane] = Ic0[ch];
+                zs.P[ch][lane] = P0[ch];
+            }
+            zs.max_tau[lane] = tau0;
+            zs.nsamples[lane] = n0;
+        }
+        if (sampled) {
+            // sample_f32's fold, term for term
+            const float w = -dt * rc.L_unit;
+            float max_tau = zs.max_tau[lane];
+#pragma unroll
+            for (int ch = 0; ch < MK_MAX_NU; ch++) {
+                if (ch < rc.nnu) {
+                    const float I = zs.I[ch][lane], Ic = zs.Ic[ch][lane];
+                    const float tau = w * ab[ch];
+                    const float y = (w * em[ch]) * zs.P[ch][lane] - Ic;
+                    const float t = I + y;
+                    zs.Ic[ch][lane] = (t - I) - y;
+                    zs.I[ch][lane] = t;
+                    zs.P[ch][lane] *= (1.0f - tau);
+                    max_tau = fmaxf(max_tau, tau);
+                }
+            }
+            zs.max_tau[lane] = max_tau;
+            ++zs.nsamples[lane];
             if (flags & ZM_ZONE) ++zone_samples;
             ++b_samples;
         }
-        if (flags & ZM_END)
-            finish_ray_f32(reqs[rq], pix, I, Ic, msg.steps[b][lane], msg.why[b][lane], nsamples, max_tau, ws);
-        if (flags & ZM_DONE) break;
+        if (flags & ZM_END) {
+            float I[MK_MAX_NU], Ic[MK_MAX_NU];
+#pragma unroll
+            for (int ch = 0; ch < MK_MAX_NU; ch++) { I[ch] = zs.I[ch][lane]; Ic[ch] = zs.Ic[ch][lane]; }
+            finish_ray_f32(reqs[rq], pix, I, Ic, steps, why, zs.nsamples[lane], zs.max_tau[lane], ws);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();  // this warp's sums before the counter
+            *(volatile int *)&zs.folded = j + 1;
+        }
+        if (__any_sync(FULL, (flags & ZM_DONE) != 0u)) break;
     }
     if (zone_samples) atomicAdd(&ws->samples_fp64, (unsigned long long)zone_samples);
     if (b_samples) atomicAdd(&ws->samples_b, (unsigned long long)b_samples);
@@ -956,18 +1163,24 @@ __device__ __forceinline__ void zone_sample(const mk_request *__restrict__ reqs,
 
 __global__ void __launch_bounds__(ZONE_THREADS)
 render_zone_kernel(const mk_request *__restrict__ reqs, const mk_snapshot_view *__restrict__ snaps,
-                   RenderWorkspace *ws, const RayRecord *q64, long long capacity, int escape) {
-    __shared__ ZoneMsgs msg;
-    // warps 0 and 2 of a 4-warp block: 4-warp blocks spread the pairs over
-    // the SMs' sub-partitions better than 2-warp blocks (measured ~5 %);
-    // warps 1 and 3 leave at once
+                   RenderWorkspace *ws, const RayRecord *q64, long long capacity, int escape,
+                   unsigned long long wait_ns, int withhold) {
+    __shared__ ZoneShared zs;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ZONE_SLOTS; s++) {
+            mbar_init(&zs.full[s], 32);
+            mbar_init(&zs.empty[s], 32);
+        }
+        zs.folded = 0;
+        zs.abort = 0;
+    }
+    __syncthreads();
     const int w = threadIdx.x >> 5;
     if (w == 0)
-        zone_integrate(reqs, snaps, ws, q64, capacity, escape, msg);
-    else if (w == 2)
-        zone_sample(reqs, snaps, ws, q64, msg);
+        zone_integrate(reqs, snaps, ws, q64, capacity, escape, zs, wait_ns, withhold);
+    else
+        zone_sample(w - 1, reqs, snaps, ws, q64, zs, wait_ns);
 }
-
 
 // Initial states of every camera ray of a launch, in FP64 (camera_ray),
 // for mixed-form launches larger than one wave of phase A: there each thread
@@ -1210,6 +1423,17 @@ extern "C" int mk_set_tuning(const char *name, int64_t value) {
         g_escape_cut = (int)value;
         return MK_OK;
     }
+    if (!strcmp(name, "zone_wait_ns")) {
+        MK_REQUIRE(value >= 1 && value <= 60000000000ll, MK_ERR_ARG,
+                   "mk_set_tuning: zone_wait_ns must lie in 1 .. 6e10");
+        g_zone_wait_ns = (unsigned long long)value;
+        return MK_OK;
+    }
+    if (!strcmp(name, "zone_wait_test")) {
+        MK_REQUIRE(value == 0 || value == 1, MK_ERR_ARG, "mk_set_tuning: zone_wait_test must be 0 or 1");
+        g_zone_wait_test = (int)value;
+        return MK_OK;
+    }
     if (!strcmp(name, "fp64_zone")) {
         MK_REQUIRE(value == 0 || value == 1, MK_ERR_ARG, "mk_set_tuning: fp64_zone must be 0 or 1");
         g_fp64_zone = (int)value;
@@ -1326,7 +1550,9 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
         MK_CUDA(cudaEventRecord(side->fork, st));
         MK_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
         render_zone_kernel<<<(unsigned)device_sm_count() * 4, ZONE_THREADS, 0, st>>>(reqs_dev, snaps_dev, ws, q64,
-                                                                                      cap, g_escape_cut);
+                                                                                      cap, g_escape_cut,
+                                                                                      g_zone_wait_ns,
+                                                                                      g_zone_wait_test);
         MK_LAUNCHED("render_zone_kernel");
         launch_f32_queue(side->s);
         MK_LAUNCHED("render_f32_kernel (queue)");

@@ -142,6 +142,16 @@ class PreparedRender:
                   self.nsnap, self.precision, ptr(self.ws), self.ws.numel() * 8, stream_ptr(stream))
         return self.images
 
+    def check(self):
+        """Raise MKError (MK_ERR_TIMEOUT) if a bounded wait of the last
+        launch's near-hole pipeline ran out, which leaves its images invalid
+        (syncs).  Never expected; the limit only keeps a fault from hanging
+        the GPU."""
+        n = int(self.ws[_lib.MK_WS_ERROR].item())
+        if n:
+            raise _lib.MKError(_lib.MK_ERR_TIMEOUT,
+                               f"mk_render: {n} waits of the near-hole pipeline ran out; the images are invalid")
+
     def work_totals(self):
         """(accepted steps, in-snapshot samples) of the last launch (syncs)."""
         w = self.ws[:32].cpu()
@@ -186,9 +196,11 @@ def render_requests(requests, precision="fp64", stream=None, with_steps=False):
     """Render several requests in ONE persistent launch.
 
     Each request's ``out`` dict receives ``image`` ((nnu, res, res) float64
-    CUDA tensor) and, with ``with_steps``, ``nsteps`` and ``status``.
-    Returns the list of image tensors.  The launch is asynchronous on
-    ``stream`` (default: the current stream)."""
+    CUDA tensor), ``check`` (PreparedRender.check of the launch: raises if
+    a wait of the mixed form's near-hole pipeline ran out; syncs) and, with
+    ``with_steps``, ``nsteps`` and ``status``.  Returns the list of image
+    tensors.  The launch is asynchronous on ``stream`` (default: the current
+    stream)."""
     if not requests:
         return []
     s = stream if stream is not None else torch.cuda.current_stream()
@@ -198,6 +210,8 @@ def render_requests(requests, precision="fp64", stream=None, with_steps=False):
     # the request table and workspace stay alive until the launch retires
     for t in (prep.reqs_dev, prep.snaps_dev, prep.ws):
         t.record_stream(s)
+    for r in requests:
+        r.out["check"] = prep.check
     return images
 
 
@@ -208,8 +222,13 @@ def make_image(fluid_model, camera_inclination=60, camera_distance=1000, mass_sc
     with a list of frequencies, (nnu, resolution, resolution)."""
     req = RenderRequest(fluid_model, camera_inclination, camera_distance, mass_scale, M_bh, r_high,
                         observing_frequency, fov, resolution, max_nsteps, r_low)
-    img = render_requests([req], precision=precision)[0]
+    s = torch.cuda.current_stream()
+    with torch.cuda.stream(s):
+        prep = PreparedRender([req], precision)
+        img = prep.launch(s)[0]
     out = img.cpu().numpy()
+    if prep.precision == _lib.MK_MIXED:
+        prep.check()
     if np.ndim(observing_frequency) == 0:
         out = out[0]
     return out

@@ -454,15 +454,21 @@ class DeviceExecutor:
             host = [torch.empty(img.shape, dtype=img.dtype, pin_memory=True) for img in images]
             for h, img in zip(host, images):
                 h.copy_(img, non_blocking=True)
+            # the near-hole pipeline's count of waits that ran out (MK_WS_ERROR)
+            err = torch.empty(1, dtype=torch.int64, pin_memory=True)
+            err.copy_(buf["ws"][_lib.MK_WS_ERROR:_lib.MK_WS_ERROR + 1], non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(stream)
-        return dict(event=ev, host=host, images=images, error=None)
+        return dict(event=ev, host=host, images=images, error=None, wait_errors=err)
 
     def poll(self, handle):
         if handle.get("error") is not None:
             return dict(ok=False, error=handle["error"], images=None)
         if not handle["event"].query():
             return None
+        if int(handle["wait_errors"][0]):
+            return dict(ok=False, images=None,
+                        error=f"[mk_status {_lib.MK_ERR_TIMEOUT}] a wait of the near-hole pipeline ran out")
         return dict(ok=True, error=None, images=[h.numpy().copy() for h in handle["host"]])
 
 

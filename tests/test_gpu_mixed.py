@@ -243,3 +243,30 @@ def test_escape_cut_leaves_images_bit_identical(cuda, medium_model, precision):
     moved = na != nb
     assert moved.any() and np.all(na[moved] < nb[moved]) and np.all(sa[moved] == _lib.MK_RAY_ESCAPED)
     assert cut.work_totals()[0] < full.work_totals()[0]
+
+
+def test_near_hole_wait_limit_ends_a_stalled_pipeline(cuda, medium_model):
+    """Every wait between the warps of MK_MIXED's near-hole pipeline is
+    bounded.  With the integrating warps withholding their first message
+    (the "zone_wait_test" switch), each block's first sampler waits on a
+    phase nothing completes: the wait runs out after zone_wait_ns, the block
+    aborts, the kernel returns, the workspace header counts the waits that
+    ran out and make_image raises MK_ERR_TIMEOUT.  The next render is the
+    normal image again, bit for bit."""
+    from mahakala_gb300 import _lib, configs
+    from mahakala_gb300.images import make_image
+    kw = dict(camera_inclination=17.0, mass_scale=configs.mass_scale_for(40.0), M_bh=6.5e9 * 1.989e33,
+              r_high=40.0, observing_frequency=230e9, fov=50.0, resolution=32, max_nsteps=8192,
+              precision="mixed")
+    ref = make_image(medium_model, **kw)
+    try:
+        _lib.call("mk_set_tuning", b"zone_wait_ns", 2_000_000)
+        _lib.call("mk_set_tuning", b"zone_wait_test", 1)
+        with pytest.raises(_lib.MKError) as e:
+            make_image(medium_model, **kw)
+        assert e.value.code == _lib.MK_ERR_TIMEOUT
+    finally:
+        _lib.call("mk_set_tuning", b"zone_wait_test", 0)
+        _lib.call("mk_set_tuning", b"zone_wait_ns", 1_000_000_000)
+    again = make_image(medium_model, **kw)
+    assert np.array_equal(again, ref, equal_nan=True)
