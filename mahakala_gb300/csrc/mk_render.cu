@@ -28,9 +28,9 @@
 //        ray moving outward past R_TURN is parked in the FP32 queue (records
 //        in binary64);
 //     B  the near-hole queue (render_zone_kernel): the float-pair state is
-//        renormalised to null in binary64 on entry, at each radial turning
-//        point and when the ray leaves R_TURN outward; the kernel carries the
-//        ray on to its end;
+//        renormalised to null in binary64 on entry and at each radial
+//        turning point inside R_TURN; the kernel carries the ray on to its
+//        end;
 //     C  the FP32 queue (render_f32_kernel over the queue), beside B: the
 //        two share no ray and no counter.
 //   MK_MIXED_STRICT: phase B integrates the near-hole geodesic entirely in
@@ -710,8 +710,8 @@ __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix,
 // Mixed-form phase B (MK_MIXED): the rays near the hole.  The state is a
 // float pair per component (~48-bit significand), advanced by RK4
 // increments formed in float (rk4_increment_f32); the wavevector is
-// renormalised to null in binary64 on entry, at every radial turning point
-// and on leaving R_TURN outward; the intensity and transmission sums are
+// renormalised to null in binary64 on entry and at every radial turning
+// point inside R_TURN; the intensity and transmission sums are
 // compensated floats.  The accelerations and the emission are float, as in
 // phase A: on this part a binary64 acceleration costs ~33x a float one per
 // step, and over the measured images it changed the error against the FP64
@@ -856,10 +856,10 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
     bool active = false, exhausted = false;
     int steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0, b_steps = 0, ray = -1;
     // float-pair state (X, K) throughout, as in the FP32 phases; near the
-    // hole the wavevector is renormalised to null in binary64 on entry, at
-    // every radial turning point and on the way out.  After the ray leaves
-    // outward the integration continues here to the ray's end (its
-    // remaining ~250 steps would otherwise wait for a third launch).
+    // hole the wavevector is renormalised to null in binary64 on entry and
+    // at every radial turning point.  After the ray leaves outward the
+    // integration continues here to the ray's end (its remaining ~250 steps
+    // would otherwise wait for a third launch).
     bool inzone = true;
     double bhspin = 0.0;
     f2 X[4], K[4];
@@ -980,18 +980,20 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                     msg.why[lane] = MK_RAY_ESCAPED;
                     msg.steps[lane] = steps;
                     active = false;
-                } else if (inzone && ((r_new >= (float)R_TURN && dr > 0.0f) ||
-                                      (dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f))) {
-                    // outbound past the photon-ring region, or a radial turning
-                    // point: renormalise to null in binary64 and re-evaluate the
-                    // first stage of the next step there
+                } else if (inzone && r_new >= (float)R_TURN && dr > 0.0f) {
+                    // outbound past the photon-ring region: on to the ray's end
+                    // in float pairs, as phase C continues its parked rays,
+                    // with no renormalisation (one here changed no pixel by
+                    // more than 1.5e-9 of its value at 256x256 and cost the
+                    // chain ~6 k cycles per ray)
+                    inzone = false;
+                    atomicAdd(&ws->zone_exits, 1ull);
+                } else if (inzone && ((dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f))) {
+                    // a radial turning point: renormalise to null in binary64
+                    // and re-evaluate the first stage of the next step there
                     renull_pair(X, K, bhspin);
                     xf[4] = K[0].hi;
                     kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3]);
-                    if (r_new >= (float)R_TURN && dr > 0.0f) {
-                        inzone = false;
-                        atomicAdd(&ws->zone_exits, 1ull);
-                    }
                 }
                 r_cur = r_new;
                 dr_prev = dr;
