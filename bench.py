@@ -53,11 +53,13 @@ FLOP_PER_EXTRA_NU = 41
 L2_FLUSH_BYTES = 256 << 20
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# each mixed-form kernel (phases A, B, C) on the 256x256 workload, from one
-# capture of `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,
-# gpu__time_duration.sum -k regex:render_ -s 9 -c 3` over
+# each mixed-form kernel (phases A, B, C) on the 256x256 workload: A and C
+# from one capture of `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,
+# gpu__time_duration.sum -k regex:render_ -s 9 -c 3`, B (the four-warp
+# near-hole pipeline) from `ncu --set full -k regex:render_zone_kernel -s 3
+# -c 1`, both over
 # `python bench.py --precision mixed --steps 2 --warmup 3 --quick --serving 0 --sampling-rays 0`
-NCU_TRAFFIC_RENDER256 = {"A": 106.92e6 + 3.01e6, "B": 76.73e6 + 0.04e6, "C": 113.40e6 + 0.16e6}
+NCU_TRAFFIC_RENDER256 = {"A": 106.92e6 + 3.01e6, "B": 76.75e6 + 1.63e6, "C": 113.40e6 + 0.16e6}
 
 # FP64 FLOP (DFMA = 2) per point of the standalone sampling stage, from ncu's
 # DADD/DMUL/DFMA thread-instruction counters on fluid_scalars_kernel (64x64
@@ -845,8 +847,9 @@ def main():
             out["traffic_note"] = ("ncu on the 192x192 case: 242 MB DRAM read per launch; the kernel is "
                                    "FP64-pipe bound (71 % FP64 pipe, 0.04 % DRAM)")
         else:
-            out["note"] = ("phase B runs the serial chain of its longest ray (zone_run_max steps) on one warp "
-                           "per sub-partition: latency-bound, not throughput-bound")
+            out["note"] = ("phase B runs the serial chain of its longest ray (zone_run_max steps): one integrating "
+                           "warp per block, three sampling warps beside it on the other sub-partitions; "
+                           "latency-bound, not throughput-bound")
         return out
 
     def form_line(form):
