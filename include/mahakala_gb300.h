@@ -364,7 +364,9 @@ int mk_render_job(const mk_job *job_dev, const mk_request *reqs_dev, const mk_sn
    first call on a device looks the array up (cudaGetSymbolAddress) and
    should come before any stream capture; a later call that finds another
    CUDA context current on that device (after a reset) looks it up again.
-   All calls share the array: calls that overlap on the GPU race. */
+   All calls share the array: calls that overlap on the GPU race.  The
+   workspace header, MK_WS_ERROR included, stays inside the library: a
+   near-hole wait that ran out (never expected) is not reported here. */
 #define MK_NOALLOC_WORKSPACE_BYTES (16u << 20)
 #define MK_NOALLOC_MAX_MIXED_RAYS ((MK_NOALLOC_WORKSPACE_BYTES - 256u) / 320u)
 int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_rays,
