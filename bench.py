@@ -914,11 +914,11 @@ def main():
         "cpu_baseline": {"value": cpu_val, "unit": "rays/s", "cores": threads, "kind": "port",
                          "sample": cpu_sample},
         "e2e": {"value": world * rays / e2e_t, "unit": "rays/s", "h2d_bytes_per_step": len(res[head]["prep"].table_bytes),
-                "d2h_bytes_per_step": int(rays * nnu * 8),
+                "d2h_bytes_per_step": int(rays * nnu * 8) + 8,  # the image and the launch's wait-error word
                 "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
         "e2e_fp64": ({"value": world * rays / e2e64_t, "unit": "rays/s",
                       "h2d_bytes_per_step": len(res["fp64"]["prep"].table_bytes),
-                      "d2h_bytes_per_step": int(rays * nnu * 8),
+                      "d2h_bytes_per_step": int(rays * nnu * 8) + 8,
                       "api": "mahakala_gb300.images.make_image(precision='fp64') (host request -> NumPy image)"}
                      if e2e64_times else None),
         "fp64_vs_reference": ({"e2e_ratio": (world * rays / e2e64_t) / cpu_val,

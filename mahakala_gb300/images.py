@@ -129,7 +129,12 @@ class PreparedRender:
             offset += r.npx
         self.total_rays = offset
         self.table_bytes = bytes(table)
-        self.reqs_dev = torch.frombuffer(bytearray(self.table_bytes), dtype=torch.uint8).to(dev)
+        # the request table goes up from pinned memory, asynchronously on the
+        # current stream (a pageable copy stages through the driver and
+        # blocks the host); the pinned block stays with this object
+        self._table_host = torch.frombuffer(bytearray(self.table_bytes), dtype=torch.uint8).pin_memory()
+        self.reqs_dev = torch.empty(len(self.table_bytes), dtype=torch.uint8, device=dev)
+        self.reqs_dev.copy_(self._table_host, non_blocking=True)
         self.snaps_dev = torch.cat([sn.view_dev for sn in snaps]) if len(snaps) > 1 else snaps[0].view_dev
         self.nsnap = len(snaps)
         nbytes = _lib.load().mk_render_workspace_bytes(self.total_rays, self.precision)
@@ -226,9 +231,17 @@ def make_image(fluid_model, camera_inclination=60, camera_distance=1000, mass_sc
     with torch.cuda.stream(s):
         prep = PreparedRender([req], precision)
         img = prep.launch(s)[0]
-    out = img.cpu().numpy()
-    if prep.precision == _lib.MK_MIXED:
-        prep.check()
+        # the image and the launch's wait-error word come back into pinned
+        # memory behind the render, then one synchronisation
+        out_host = torch.empty(img.shape, dtype=img.dtype, pin_memory=True)
+        out_host.copy_(img, non_blocking=True)
+        err = torch.empty(1, dtype=torch.int64, pin_memory=True)
+        err.copy_(prep.ws[_lib.MK_WS_ERROR:_lib.MK_WS_ERROR + 1], non_blocking=True)
+    s.synchronize()
+    if int(err[0]):
+        raise _lib.MKError(_lib.MK_ERR_TIMEOUT, f"mk_render: {int(err[0])} waits of the near-hole pipeline ran out; "
+                                                "the image is invalid")
+    out = out_host.numpy()
     if np.ndim(observing_frequency) == 0:
         out = out[0]
     return out
