@@ -52,6 +52,13 @@ FLOP_PER_EXTRA_NU = 41
 
 L2_FLUSH_BYTES = 256 << 20
 
+# cycles per RK4 step of one warp alone running the near-hole phase's
+# integration step (four float accelerations, the stage combinations and the
+# float-pair state update; GB300, clock64 over 400 steps of 32 rays from the
+# near-hole queue of the 256x256 render): the latency floor of phase B's
+# serial chain
+CHAIN_FLOOR_CYCLES = 1270
+
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # each mixed-form kernel (phases A, B, C) on the 256x256 workload: A and C
 # from one capture of `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,
@@ -850,6 +857,18 @@ def main():
             out["note"] = ("phase B runs the serial chain of its longest ray (zone_run_max steps): one integrating "
                            "warp per block, three sampling warps beside it on the other sub-partitions; "
                            "latency-bound, not throughput-bound")
+            if form == "mixed" and r["zone_run_max"]:
+                # the bound that applies to a serial chain: cycles per step of
+                # its integrating warp against that warp's RK4 step alone
+                mhz = (clocks or {}).get("sm_mhz") or sm_max_mhz(local) or float("nan")
+                cps = tB * mhz * 1e6 / r["zone_run_max"]
+                out["chain"] = {"steps": r["zone_run_max"], "cycles_per_step": cps,
+                                "floor_cycles_per_step": CHAIN_FLOOR_CYCLES, "frac": CHAIN_FLOOR_CYCLES / cps,
+                                "sm_mhz": mhz,
+                                "floor_source": ("one warp alone running the integrating warp's RK4 step (four float "
+                                                 "accelerations, stage combinations, float-pair state update) on "
+                                                 "GB300, clock64 over 400 steps; the phase's time over zone_run_max "
+                                                 "steps at the sampled SM clock gives cycles_per_step")}
         return out
 
     def form_line(form):
