@@ -803,6 +803,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 __device__ __forceinline__ bool zone_wait(unsigned long long *b, unsigned parity, const ZoneShared &zs,
                                           unsigned long long limit_ns) {
     const unsigned FULL = 0xffffffffu;
+    // the common case, a phase already complete, reads no timer
+    if (__all_sync(FULL, mbar_test(b, parity))) return true;
     const unsigned long long t0 = global_ns();
     for (unsigned i = 1;; ++i) {
         if (__all_sync(FULL, mbar_test(b, parity))) return true;
@@ -816,6 +818,10 @@ __device__ __forceinline__ bool zone_wait(unsigned long long *b, unsigned parity
 // Bounded wait of a whole warp until `folded` reads j.
 __device__ __forceinline__ bool zone_wait_fold(const ZoneShared &zs, int j, unsigned long long limit_ns) {
     const unsigned FULL = 0xffffffffu;
+    if (__all_sync(FULL, *(const volatile int *)&zs.folded == j)) {
+        __threadfence_block();  // the sums written before `folded` was set
+        return true;
+    }
     const unsigned long long t0 = global_ns();
     for (unsigned i = 1;; ++i) {
         if (__all_sync(FULL, *(const volatile int *)&zs.folded == j)) {
