@@ -380,7 +380,8 @@ int mk_render_noalloc(const mk_request *reqs_dev, int32_t nreq, int64_t total_ra
    "f32_blocks_per_sm" (0, 3, 4 or 5; default 0): the FP32 phases' kernels
    compiled for 3 resident blocks per SM (no register spills), 4 (128
    registers) or 5 (96 registers); 0 takes 4 when the launch's rays fit one
-   wave of 4-block slots and 5 otherwise.
+   wave of 4-block slots and 5 otherwise, and 3 for MK_MIXED's FP32
+   continuation, which runs beside the near-hole phase.
    "escape_cut" (0 or 1; default 1): the mixed forms end outbound rays
    beyond the snapshot's bounding radius (see mk_precision).
    "phase_events" (0 or 1; default 0): renders record CUDA events on their

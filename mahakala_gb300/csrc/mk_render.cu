@@ -1531,7 +1531,7 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     // MK_MIXED's FP32 queue holds parked phase-A rays; the other mixed forms'
     // hold the near-hole phase's exits
     const int qmode = (precision == MK_MIXED ? 0 : F32_RENULL) | (g_escape_cut ? F32_ESCAPE : 0);
-    auto launch_f32_queue = [&](cudaStream_t s) {
+    auto launch_f32_queue = [&](cudaStream_t s, int f32_blocks) {
         if (f32_blocks == 5)
             render_f32_kernel<SRC_QUEUE, 5>
                 <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 5>, 6), max_rays), RENDER_THREADS, 0,
@@ -1562,7 +1562,12 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
                                                                                       g_zone_wait_ns,
                                                                                       g_zone_wait_test);
         MK_LAUNCHED("render_zone_kernel");
-        launch_f32_queue(side->s);
+        // beside the near-hole pipeline (168 registers a thread) phase C runs
+        // its spill-free 3-block build unless a tuning asks otherwise (phase
+        // C 0.92 -> 0.84 ms at 256x256, 11.1 -> 10.9 ms on the 1024x1024
+        // stress render, against the 128-register 4-block and 96-register
+        // 5-block builds, which spill)
+        launch_f32_queue(side->s, g_f32_blocks ? f32_blocks : 3);
         MK_LAUNCHED("render_f32_kernel (queue)");
         if ((rc = phase_mark(st, 2)) != MK_OK) return rc;
         if ((rc = phase_mark(side->s, 3, 1)) != MK_OK) return rc;
@@ -1583,7 +1588,7 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
         MK_LAUNCHED("render_fp64_kernel (queue)");
     }
     if ((rc = phase_mark(st, 2)) != MK_OK) return rc;
-    launch_f32_queue(st);
+    launch_f32_queue(st, f32_blocks);
     MK_LAUNCHED("render_f32_kernel (queue)");
     return phase_mark(st, 3);
 }
