@@ -83,7 +83,8 @@ def test_tuning_switches_validate_without_gpu(lib):
     others (no GPU call is made)."""
     from mahakala_gb300 import _lib
     for name, good, bad in ((b"fp64_rays_per_warp", (1, 32), (3, 64)), (b"fp64_zone", (0, 1), (2,)),
-                            (b"phase_events", (1, 0), (5,)), (b"f32_blocks_per_sm", (0, 3, 4, 5), (2, 6))):
+                            (b"phase_events", (1, 0), (5,)), (b"f32_blocks_per_sm", (0, 3, 4, 5), (2, 6)),
+                            (b"zone_wait_test", (1, 0), (2,)), (b"zone_wait_ns", (5, 1_000_000_000), (0,))):
         for v in good:
             _lib.call("mk_set_tuning", name, v)
         for v in bad:
@@ -94,6 +95,8 @@ def test_tuning_switches_validate_without_gpu(lib):
     _lib.call("mk_set_tuning", b"fp64_zone", 1)
     _lib.call("mk_set_tuning", b"phase_events", 0)
     _lib.call("mk_set_tuning", b"f32_blocks_per_sm", 0)
+    _lib.call("mk_set_tuning", b"zone_wait_test", 0)
+    _lib.call("mk_set_tuning", b"zone_wait_ns", 1_000_000_000)
     with pytest.raises(_lib.MKError):
         _lib.call("mk_set_tuning", b"no_such_knob", 1)
 
