@@ -776,35 +776,37 @@ def main():
         stress = stress_record(torch, stream, flush, peaks)
 
     # end to end through the public API: host request in, NumPy image out
-    # (W untimed calls first, like the device timing)
-    e2e_times = []
-    for k in range(0 if args.quick else max(args.warmup, 3) + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        img_np = make_image(model, camera_inclination=spec.inclination, camera_distance=spec.camera_distance,
-                            mass_scale=spec.mass_scale, M_bh=spec.M_bh, r_high=spec.r_high,
-                            observing_frequency=list(spec.freqs) if nnu > 1 else spec.freqs[0], fov=spec.fov,
-                            resolution=spec.resolution, max_nsteps=spec.max_nsteps, precision=head)
-        if k >= max(args.warmup, 3):
-            e2e_times.append(time.perf_counter() - t0)
-    e2e_t = statistics.mean(e2e_times) if e2e_times else float("nan")
-    # the FP64 form end to end too (like for like against the FP64 CPU path)
-    e2e64_times = []
-    if head != "fp64" and "fp64" in forms:
+    # (W untimed calls first, like the device timing).  Each timed call is
+    # preceded, outside the timed region, by the same L2 flush as the
+    # device-timed steps, so both measure from the same GPU state; the same
+    # calls back to back with no flush are reported beside it
+    # (e2e_back_to_back)
+    def e2e_series(precision, flushed):
+        out = []
         for k in range(0 if args.quick else max(args.warmup, 3) + args.steps):
+            if flushed:
+                flush.fill_(1.0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             make_image(model, camera_inclination=spec.inclination, camera_distance=spec.camera_distance,
                        mass_scale=spec.mass_scale, M_bh=spec.M_bh, r_high=spec.r_high,
                        observing_frequency=list(spec.freqs) if nnu > 1 else spec.freqs[0], fov=spec.fov,
-                       resolution=spec.resolution, max_nsteps=spec.max_nsteps, precision="fp64")
+                       resolution=spec.resolution, max_nsteps=spec.max_nsteps, precision=precision)
             if k >= max(args.warmup, 3):
-                e2e64_times.append(time.perf_counter() - t0)
+                out.append(time.perf_counter() - t0)
+        return out
+
+    e2e_times = e2e_series(head, True)
+    e2e_t = statistics.mean(e2e_times) if e2e_times else float("nan")
+    e2e_b2b = e2e_series(head, False)
+    e2e_b2b_t = statistics.mean(e2e_b2b) if e2e_b2b else float("nan")
+    # the FP64 form end to end too (like for like against the FP64 CPU path)
+    e2e64_times = e2e_series("fp64", True) if head != "fp64" and "fp64" in forms else []
     e2e64_t = statistics.mean(e2e64_times) if e2e64_times else float("nan")
     if world > 1 and e2e_times:  # the slowest replica sets the job's rate
-        t = torch.tensor([e2e_t, e2e64_t], device="cuda")
+        t = torch.tensor([e2e_t, e2e64_t, e2e_b2b_t], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_t, e2e64_t = float(t[0].item()), float(t[1].item())
+        e2e_t, e2e64_t, e2e_b2b_t = float(t[0].item()), float(t[1].item()), float(t[2].item())
     L_unit = model.get_units(spec.M_bh, spec.mass_scale)["L_unit"]
 
     def roofline(form):
@@ -934,11 +936,15 @@ def main():
                          "sample": cpu_sample},
         "e2e": {"value": world * rays / e2e_t, "unit": "rays/s", "h2d_bytes_per_step": len(res[head]["prep"].table_bytes),
                 "d2h_bytes_per_step": int(rays * nnu * 8) + 8,  # the image and the launch's wait-error word
-                "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)"},
+                "api": f"mahakala_gb300.images.make_image(precision='{head}') (host request -> NumPy image)",
+                "l2": "flushed before each call (256 MB write, untimed), as the device-timed steps"},
+        "e2e_back_to_back": {"value": world * rays / e2e_b2b_t, "unit": "rays/s",
+                             "note": "the same make_image calls back to back, no flush between them"},
         "e2e_fp64": ({"value": world * rays / e2e64_t, "unit": "rays/s",
                       "h2d_bytes_per_step": len(res["fp64"]["prep"].table_bytes),
                       "d2h_bytes_per_step": int(rays * nnu * 8) + 8,
-                      "api": "mahakala_gb300.images.make_image(precision='fp64') (host request -> NumPy image)"}
+                      "api": "mahakala_gb300.images.make_image(precision='fp64') (host request -> NumPy image)",
+                      "l2": "flushed before each call (256 MB write, untimed)"}
                      if e2e64_times else None),
         "fp64_vs_reference": ({"e2e_ratio": (world * rays / e2e64_t) / cpu_val,
                                "device_ratio": (world * rays / res["fp64"]["t_step"]) / cpu_val,
