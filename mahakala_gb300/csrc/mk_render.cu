@@ -1229,7 +1229,11 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
         nreq = job->nreq;
         total_camera = job->total_rays;
     }
-    __shared__ ReqF32 s_req[MK_MAX_REQUESTS_MIXED];
+    // the requests' float constants, sized at launch by the request count
+    // (MK_MAX_REQUESTS_MIXED for a job read from the device): shared memory
+    // the table does not take stays L1 for the gathers
+    extern __shared__ __align__(16) unsigned char s_req_raw[];
+    ReqF32 *s_req = reinterpret_cast<ReqF32 *>(s_req_raw);
     for (int q = threadIdx.x; q < min(nreq, MK_MAX_REQUESTS_MIXED); q += blockDim.x) fill_req_f32(reqs[q], snaps, s_req[q]);
     __syncthreads();
     unsigned long long *counter = SRC == SRC_CAMERA ? &ws->counter : &ws->q32_next;
@@ -1512,17 +1516,20 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     // the near-hole phase instead of after it
     const int mode = (g_fp64_zone ? F32_HANDOFF : 0) | (precision == MK_MIXED ? F32_PARK : 0) |
                      (g_escape_cut ? F32_ESCAPE : 0);
+    // dynamic shared memory of the FP32 kernels: their request table
+    const size_t req_smem =
+        (size_t)(job_dev ? MK_MAX_REQUESTS_MIXED : std::min<int32_t>(nreq, MK_MAX_REQUESTS_MIXED)) * sizeof(ReqF32);
     if (f32_blocks == 5)
         render_f32_kernel<SRC_CAMERA, 5>
-            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 5>, 5), max_rays), RENDER_THREADS, 0,
+            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 5>, 5), max_rays), RENDER_THREADS, req_smem,
                st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode, cam);
     else if (f32_blocks == 4)
         render_f32_kernel<SRC_CAMERA, 4>
-            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 4>, 1), max_rays), RENDER_THREADS, 0,
+            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 4>, 1), max_rays), RENDER_THREADS, req_smem,
                st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode, cam);
     else
         render_f32_kernel<SRC_CAMERA, 3>
-            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 3>, 2), max_rays), RENDER_THREADS, 0,
+            <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_CAMERA, 3>, 2), max_rays), RENDER_THREADS, req_smem,
                st>>>(reqs_dev, nreq, (long long)total_rays, snaps_dev, ws, q64, q32, cap, job_dev, mode, cam);
     MK_LAUNCHED("render_f32_kernel (camera)");
     if ((rc = phase_mark(st, 1)) != MK_OK) return rc;
@@ -1534,15 +1541,15 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     auto launch_f32_queue = [&](cudaStream_t s, int f32_blocks) {
         if (f32_blocks == 5)
             render_f32_kernel<SRC_QUEUE, 5>
-                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 5>, 6), max_rays), RENDER_THREADS, 0,
+                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 5>, 6), max_rays), RENDER_THREADS, req_smem,
                    s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, qmode, nullptr);
         else if (f32_blocks == 4)
             render_f32_kernel<SRC_QUEUE, 4>
-                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 4>, 3), max_rays), RENDER_THREADS, 0,
+                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 4>, 3), max_rays), RENDER_THREADS, req_smem,
                    s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, qmode, nullptr);
         else
             render_f32_kernel<SRC_QUEUE, 3>
-                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 3>, 4), max_rays), RENDER_THREADS, 0,
+                <<<persistent_grid(blocks_per_sm(render_f32_kernel<SRC_QUEUE, 3>, 4), max_rays), RENDER_THREADS, req_smem,
                    s>>>(reqs_dev, nreq, 0, snaps_dev, ws, q64, q32, cap, job_dev, qmode, nullptr);
     };
     // The near-hole queue: persistent grids, small blocks, so the few rays
