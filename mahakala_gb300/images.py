@@ -129,12 +129,12 @@ class PreparedRender:
             offset += r.npx
         self.total_rays = offset
         self.table_bytes = bytes(table)
-        # the request table goes up from pinned memory, asynchronously on the
-        # current stream (a pageable copy stages through the driver and
-        # blocks the host); the pinned block stays with this object
+        # the request table goes up from pinned memory (a pageable copy
+        # stages through the driver); the copy completes before the
+        # constructor returns, so a launch on any stream finds it
         self._table_host = torch.frombuffer(bytearray(self.table_bytes), dtype=torch.uint8).pin_memory()
         self.reqs_dev = torch.empty(len(self.table_bytes), dtype=torch.uint8, device=dev)
-        self.reqs_dev.copy_(self._table_host, non_blocking=True)
+        self.reqs_dev.copy_(self._table_host)
         self.snaps_dev = torch.cat([sn.view_dev for sn in snaps]) if len(snaps) > 1 else snaps[0].view_dev
         self.nsnap = len(snaps)
         nbytes = _lib.load().mk_render_workspace_bytes(self.total_rays, self.precision)
