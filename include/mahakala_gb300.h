@@ -50,9 +50,9 @@ typedef enum {
 /* MK_FP64: every operation in binary64.
    MK_MIXED: FP32 arithmetic (ray state as float pairs, Kahan-compensated
    intensity); near the hole (r < 3 M, or inbound inside 6 M where
-   photon-ring rays turn) the ray state and the intensity sums are binary64
-   and the wavevector is renormalised to null in binary64 on entry, on exit
-   and at every radial turning point; accelerations and emission stay FP32.
+   photon-ring rays turn) the wavevector is renormalised to null on entry
+   (binary64) and at every radial turning point (double-float pairs, ~1e-13
+   relative); accelerations and emission stay FP32.
    MK_MIXED_STRICT: as MK_MIXED, but near the hole the whole geodesic step
    (accelerations included) is binary64.
    MK_MIXED_DF: as MK_MIXED_STRICT with that step in double-float (pairs of

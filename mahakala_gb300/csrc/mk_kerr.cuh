@@ -348,6 +348,41 @@ __device__ __forceinline__ f2 f2_from(double d) {
 
 __device__ __forceinline__ double f2_to(f2 x) { return (double)x.hi + (double)x.lo; }
 
+// x * p for p a power of two (exact)
+__host__ __device__ __forceinline__ dd dd_scale(dd x, float p) { return dd(x.hi * p, x.lo * p); }
+
+// k^t rescaled so that g(k, k) = 0 at x, keeping the spatial wavevector:
+// the root of g00 k0^2 + 2 g0i k^i k0 + gij k^i k^j = 0 nearest the current
+// k0 (g00 = f - 1, g0i k^i = f l.k, gij k^i k^j = |k|^2 + f (l.k)^2 with
+// l.k = l_i k^i), as the binary64 form of the FP64 queue phases solves it,
+// in double-float arithmetic (~44 significant bits, all on the FP32 pipe).
+// On a float-pair state the result carries no less precision than the
+// state itself.  A state with no real root, or on the surface g00 = 0, is
+// returned unchanged.
+__host__ __device__ __forceinline__ dd renull_k0_dd(dd x, dd y, dd z, dd k0, dd k1, dd k2, dd k3, dd a) {
+    const dd aa = a * a, zz = z * z;
+    const dd kk = dd_scale(x * x + y * y + zz - aa, 0.5f);
+    const dd Q = kk * kk + aa * zz;
+    const dd rr = (Q.hi > 0.0f ? Q * inv_sqrt(Q) : dd(0.0f)) + kk;  // r^2
+    const dd ir = inv_sqrt(rr);
+    const dd r = rr * ir;
+    const dd den = rr * rr + aa * zz, rra = rr + aa;
+    const dd inv2 = dd(1.0f) / (den * rra);  // 1 / ((r^4 + a^2 z^2)(r^2 + a^2))
+    const dd f = dd_scale(rr * r * (rra * inv2), 2.0f);
+    const dd ira = den * inv2;  // 1 / (r^2 + a^2)
+    const dd l1 = (r * x + a * y) * ira, l2 = (r * y - a * x) * ira, l3 = z * ir;
+    const dd lk = l1 * k1 + l2 * k2 + l3 * k3;
+    const dd A = f - dd(1.0f);
+    const dd B = dd_scale(f * lk, 2.0f);
+    const dd C = k1 * k1 + k2 * k2 + k3 * k3 + f * lk * lk;
+    const dd disc = B * B - dd_scale(A * C, 4.0f);
+    if (!(disc.hi >= 0.0f) || A.hi == 0.0f) return k0;
+    const dd sq = disc.hi > 0.0f ? disc * inv_sqrt(disc) : dd(0.0f);
+    const dd i2A = dd(1.0f) / dd_scale(A, 2.0f);
+    const dd r1 = (sq - B) * i2A, r2 = -(B + sq) * i2A;
+    return fabsf((r1 - k0).hi) < fabsf((r2 - k0).hi) ? r1 : r2;
+}
+
 // The same operations on two components at once (float2 lanes), on paired
 // FP32 instructions; every lane rounds exactly as the scalar steps above
 // (x - y is formed as fma(y, -1, x), -p as the product with -b).

@@ -841,17 +841,6 @@ __device__ __forceinline__ void zone_fail(ZoneShared &zs, RenderWorkspace *ws) {
     if ((threadIdx.x & 31) == 0) atomicAdd(&ws->zone_error, 1ull);
 }
 
-// renull_fp64 on a float-pair state: only k^t changes
-__device__ __forceinline__ void renull_pair(const f2 X[4], f2 K[4], double a) {
-    double s[8];
-    s[0] = 0.0;  // not read
-#pragma unroll
-    for (int i = 1; i < 4; i++) { s[i] = f2_to(X[i]); s[4 + i] = f2_to(K[i]); }
-    s[4] = (double)K[0].hi;  // only picks the nearer root
-    renull_fp64(s, a);
-    K[0] = f2_from(s[4]);
-}
-
 __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ reqs,
                                                const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws,
                                                const RayRecord *q64, long long capacity, int escape,
@@ -868,6 +857,7 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
     // would otherwise wait for a third launch).
     bool inzone = true;
     double bhspin = 0.0;
+    dd ad(0.0f);  // the spin as a float pair
     f2 X[4], K[4];
     float xf[8];  // the state rounded to float
     float d1[4], dt = 0.0f, r_cur = 0.0f, dr_prev = 0.0f, reh = 0.0f, a = 0.0f, div = 0.0f, tol = 0.0f;
@@ -897,6 +887,7 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
             tol = (float)R.policy.tol;
             renull_fp64(s, bhspin);
             a = (float)bhspin;
+            ad = dd(bhspin);
             reh = (float)radius_eh(bhspin);
             r_out = snap_f32(snaps[R.snapshot]).r_out;
 #pragma unroll
@@ -995,9 +986,15 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
                     inzone = false;
                     atomicAdd(&ws->zone_exits, 1ull);
                 } else if (inzone && ((dr_prev < 0.0f && dr > 0.0f) || (dr_prev > 0.0f && dr < 0.0f))) {
-                    // a radial turning point: renormalise to null in binary64
-                    // and re-evaluate the first stage of the next step there
-                    renull_pair(X, K, bhspin);
+                    // a radial turning point: renormalise to null in
+                    // double-float arithmetic and re-evaluate the first stage
+                    // of the next step there (in binary64 its ~100 FP64-pipe
+                    // instructions held the whole warp ~6.5 k cycles each
+                    // time, whichever of its lanes turned)
+                    const dd k0 = renull_k0_dd(dd(X[1].hi, X[1].lo), dd(X[2].hi, X[2].lo), dd(X[3].hi, X[3].lo),
+                                               dd(K[0].hi, K[0].lo), dd(K[1].hi, K[1].lo), dd(K[2].hi, K[2].lo),
+                                               dd(K[3].hi, K[3].lo), ad);
+                    K[0] = {k0.hi, k0.lo};
                     xf[4] = K[0].hi;
                     kerr_accel(xf[1], xf[2], xf[3], xf[4], xf[5], xf[6], xf[7], a, d1[0], d1[1], d1[2], d1[3]);
                 }

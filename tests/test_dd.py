@@ -1,6 +1,7 @@
 """Double-float arithmetic (mahakala_gb300/csrc/mk_dd.cuh) on the host:
-add, sub, mul, div and rsqrt against long double over random operands.
-Bar: 1e-13 relative (the pairs carry ~44-48 bits)."""
+add, sub, mul, div and rsqrt against long double over random operands
+(bar: 1e-13 relative, the pairs carry ~44-48 bits), and the null
+renormalisation built on it (renull_k0_dd in mk_kerr.cuh)."""
 
 import os
 import shutil
@@ -23,3 +24,21 @@ def test_double_float_accuracy(tmp_path):
     names = ["add", "sub", "mul", "div", "rsqrt"]
     for n, e in zip(names, errs):
         assert e < 1e-13, f"{n}: {e:.3e}"
+
+
+def test_double_float_null_renormalisation(tmp_path):
+    """renull_k0_dd (mk_kerr.cuh), the near-hole phase's renormalisation at
+    radial turning points, against the quadratic's nearer root in long
+    double: 1e-11 relative away from the surface g00 = 0, 1e-9 within
+    |g00| < 1e-2 (the nearer root there loses digits in any precision)."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    exe = tmp_path / "renull_check"
+    subprocess.run([nvcc, "-O2", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-I", os.path.join(ROOT, "mahakala_gb300", "csrc"), "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "renull_check.cu"), "-o", str(exe)], check=True)
+    worst, worst_g00, near = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert int(near) > 100
+    assert float(worst) < 1e-11, worst
+    assert float(worst_g00) < 1e-9, worst_g00
