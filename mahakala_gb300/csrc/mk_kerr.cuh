@@ -383,6 +383,98 @@ __host__ __device__ __forceinline__ dd renull_k0_dd(dd x, dd y, dd z, dd k0, dd 
     return fabsf((r1 - k0).hi) < fabsf((r2 - k0).hi) ? r1 : r2;
 }
 
+// sqrt in double-float: x * (1/sqrt x); 0 at 0, NaN below
+__host__ __device__ __forceinline__ dd dd_sqrt(dd x) {
+    if (x.hi > 0.0f) return x * inv_sqrt(x);
+    return dd(x.hi == 0.0f ? 0.0f : NAN);
+}
+
+// A grid camera's constants for the mixed forms' camera rays: the pixel
+// grid coord(i) = (2i + 1) step + lo in binary64, the camera's distance
+// times sin/cos of its inclination and the spin in double-float.
+struct CameraDD {
+    dd dsi, dci, ci, si, a;
+    double step, lo;
+};
+
+__host__ __device__ __forceinline__ CameraDD camera_dd(const mk_camera &c) {
+    CameraDD o;
+    o.dsi = dd(c.distance * c.sin_inc);
+    o.dci = dd(c.distance * c.cos_inc);
+    o.ci = dd(c.cos_inc);
+    o.si = dd(c.sin_inc);
+    o.a = dd(c.bhspin);
+    o.step = (c.fov_upper - c.fov_lower) / (double)(2 * c.pixels);
+    o.lo = c.fov_lower;
+    return o;
+}
+
+// the binary64 grid coordinate of grid_coord (below), rounded product then
+// rounded sum, on the device or the host
+__host__ __device__ __forceinline__ double grid_coord_of(int i, double step, double lo) {
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(__dmul_rn((double)(2 * i + 1), step), lo);
+#else
+    volatile double t = (double)(2 * i + 1) * step;
+    return t + lo;
+#endif
+}
+
+// Initial state of grid-camera pixel p as float pairs, in double-float
+// arithmetic (~1e-13 relative; the binary64 camera_ray below puts ~300
+// instructions per ray on the FP64 pipe, which every warp of the mixed
+// forms' camera phase waited on at its start).  The image-plane
+// coordinates (x, y) are the binary64 grid's (so the image centre of an odd
+// grid is exactly 0 when binary64 rounds it there); the ray starts at that
+// point moved to the camera (geodesics.py:121-132, 168-179): position
+// (d sin i - y cos i, x, y sin i + d cos i).  Its
+// direction, the cross product of the image plane's differences
+// (geodesics.py:173-176), is (x^2 + y^2)(sin i, 0, cos i) exactly: every
+// ray leaves the camera parallel to its line of sight (binary64 leaves
+// rounding residues of ~1e-13 of the components).  k^t = 1 and the spatial
+// part is rescaled to null as _Nullify does (geodesics.py:58-85, 219-230):
+// the same quadratic, the same isclose rule for a vanishing discriminant,
+// the same choice of root, NaN where there is no positive one (the image
+// centre, x = y = 0).
+__host__ __device__ __forceinline__ void camera_ray_pair(const CameraDD &c, int n, int64_t p, f2 X[4], f2 K[4]) {
+    const int ix = (int)(p / n), iy = (int)(p % n);
+    const dd x(grid_coord_of(ix, c.step, c.lo)), y(grid_coord_of(iy, c.step, c.lo));
+    const dd x1 = c.dsi - y * c.ci, x3 = y * c.si + c.dci;
+    const dd rho = x * x + y * y;
+    const dd v1 = rho * c.si, v3 = rho * c.ci;
+    // Kerr-Schild metric data at (x1, x, x3) (geodesics.py:88-104)
+    const dd a = c.a, aa = a * a, zz = x3 * x3;
+    const dd kk = dd_scale(x1 * x1 + x * x + zz - aa, 0.5f);
+    const dd rr = dd_sqrt(kk * kk + aa * zz) + kk;
+    const dd r = dd_sqrt(rr);
+    const dd f = dd_scale(rr * r, 2.0f) / (rr * rr + aa * zz);
+    const dd l1 = (r * x1 + a * x) / (rr + aa), l3 = x3 / r;
+    // g(v, v) = A (k^t)^2 + 2 b k^t + C for v = (k^t, v1, 0, v3)
+    const dd lv = l1 * v1 + l3 * v3;
+    const dd A = f - dd(1.0f), b = f * lv, C = v1 * v1 + v3 * v3 + f * lv * lv;
+    const dd bb = b * b, AC = A * C, disc = bb - AC;
+    const bool close = fabsf(disc.hi) <= 1e-8f + 1e-5f * fabsf(AC.hi);
+    const dd sq = close ? dd(0.0f) : dd_sqrt(disc);
+    const dd D = -(b.hi < 0.0f ? b : b + sq);
+    const dd q1 = D / A, q2 = C / D;
+    dd S = dd(NAN);
+    if (!(q1.hi != q1.hi) && !(q2.hi != q2.hi)) {
+        const bool lt = q1.hi < q2.hi || (q1.hi == q2.hi && q1.lo < q2.lo);
+        const dd d1 = lt ? q1 : q2, d2 = lt ? q2 : q1;
+        if (d1.hi > 0.0f) S = d1;
+        else if (d2.hi > 0.0f) S = d2;
+    }
+    const dd k1 = v1 / S, k3 = v3 / S;
+    X[0] = {0.0f, 0.0f};
+    X[1] = {x1.hi, x1.lo};
+    X[2] = {x.hi, x.lo};
+    X[3] = {x3.hi, x3.lo};
+    K[0] = {1.0f, 0.0f};
+    K[1] = {k1.hi, k1.lo};
+    K[2] = {0.0f, 0.0f};
+    K[3] = {k3.hi, k3.lo};
+}
+
 // The same operations on two components at once (float2 lanes), on paired
 // FP32 instructions; every lane rounds exactly as the scalar steps above
 // (x - y is formed as fma(y, -1, x), -p as the product with -b).
@@ -630,6 +722,22 @@ __device__ __forceinline__ void camera_ray(const mk_camera &c, int64_t p, double
     const int ix = (int)(p / n), iy = (int)(p % n);
     camera_pixel(grid_coord(ix, n, c.fov_lower, c.fov_upper), grid_coord(iy, n, c.fov_lower, c.fov_upper),
                  c.cos_inc, c.sin_inc, c.distance, c.bhspin, s);
+}
+
+// initial state of pixel p as float pairs, for the mixed forms: grid
+// cameras in double-float (camera_ray_pair), equator cameras in binary64
+__device__ __forceinline__ void camera_pair(const mk_camera &c, int64_t p, f2 X[4], f2 K[4]) {
+    if (c.kind == MK_CAMERA_GRID) {
+        camera_ray_pair(camera_dd(c), c.pixels, p, X, K);
+        return;
+    }
+    double s[8];
+    camera_ray(c, p, s);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        X[i] = f2_from(s[i]);
+        K[i] = f2_from(s[4 + i]);
+    }
 }
 
 }  // namespace mk

@@ -526,6 +526,8 @@ struct ReqF32 {
     SynchroF32 sc[MK_MAX_NU];
     SnapF32 sf;
     float a, reh;
+    CameraDD cam;           // grid camera constants for camera_ray_pair
+    int cam_pixels, cam_grid;
 };
 
 __device__ __forceinline__ void fill_req_f32(const mk_request &R, const mk_snapshot_view *snaps, ReqF32 &o) {
@@ -536,6 +538,9 @@ __device__ __forceinline__ void fill_req_f32(const mk_request &R, const mk_snaps
     o.sf = snap_f32(snaps[R.snapshot]);
     o.a = (float)R.camera.bhspin;
     o.reh = (float)radius_eh(R.camera.bhspin);
+    o.cam = camera_dd(R.camera);
+    o.cam_pixels = R.camera.pixels;
+    o.cam_grid = R.camera.kind == MK_CAMERA_GRID;
 }
 
 
@@ -710,8 +715,9 @@ __device__ __forceinline__ void finish_ray_f32(const mk_request &R, int64_t pix,
 // Mixed-form phase B (MK_MIXED): the rays near the hole.  The state is a
 // float pair per component (~48-bit significand), advanced by RK4
 // increments formed in float (rk4_increment_f32); the wavevector is
-// renormalised to null in binary64 on entry and at every radial turning
-// point inside R_TURN; the intensity and transmission sums are
+// renormalised to null on entry (binary64, from the record) and at every
+// radial turning point inside R_TURN (double-float, renull_k0_dd); the
+// intensity and transmission sums are
 // compensated floats.  The accelerations and the emission are float, as in
 // phase A: on this part a binary64 acceleration costs ~33x a float one per
 // step, and over the measured images it changed the error against the FP64
@@ -1187,15 +1193,17 @@ render_zone_kernel(const mk_request *__restrict__ reqs, const mk_snapshot_view *
         zone_sample(w - 1, reqs, snaps, ws, q64, zs, wait_ns);
 }
 
-// Initial states of every camera ray of a launch, in FP64 (camera_ray),
-// for mixed-form launches larger than one wave of phase A: there each thread
-// of phase A takes a new ray many times, and the ~270 FP64 instructions of a
-// camera ray, run for whichever lanes refill in a given step, held the
-// whole warp on the sub-partition's FP64 unit each time.  Here they run
-// once per ray, fully parallel, and phase A loads 64 bytes instead.
+// Initial states of every camera ray of a launch as float pairs (x^mu
+// then k^mu, hi and lo words: 64 B a ray), for mixed-form launches larger
+// than one wave of phase A: there each thread of phase A takes a new ray
+// many times, and the camera setup, run for whichever lanes refill in a
+// given step, held the whole warp each time.  Here it runs once per ray,
+// fully parallel, and phase A loads four 16-byte words instead.  Grid
+// cameras in double-float (camera_ray_pair), equator cameras in binary64
+// (camera_ray).
 __global__ void __launch_bounds__(RENDER_THREADS)
 camera_states_kernel(const mk_request *__restrict__ reqs, int nreq, long long total, const mk_job *job,
-                     double *__restrict__ out) {
+                     float4 *__restrict__ out) {
     if (job) {
         nreq = job->nreq;
         total = job->total_rays;
@@ -1204,10 +1212,12 @@ camera_states_kernel(const mk_request *__restrict__ reqs, int nreq, long long to
          p += (long long)gridDim.x * blockDim.x) {
         const int rq = find_request(reqs, nreq, p);
         if (!ray_in_request(reqs, nreq, p)) continue;
-        double s[8];
-        camera_ray(reqs[rq].camera, p - reqs[rq].ray_offset, s);
-#pragma unroll
-        for (int i = 0; i < 8; i++) out[8 * p + i] = s[i];
+        f2 X[4], K[4];
+        camera_pair(reqs[rq].camera, p - reqs[rq].ray_offset, X, K);
+        out[4 * p + 0] = make_float4(X[0].hi, X[0].lo, X[1].hi, X[1].lo);
+        out[4 * p + 1] = make_float4(X[2].hi, X[2].lo, X[3].hi, X[3].lo);
+        out[4 * p + 2] = make_float4(K[0].hi, K[0].lo, K[1].hi, K[1].lo);
+        out[4 * p + 3] = make_float4(K[2].hi, K[2].lo, K[3].hi, K[3].lo);
     }
 }
 
@@ -1221,7 +1231,7 @@ template <int SRC, int MINB>
 __global__ void __launch_bounds__(RENDER_THREADS, MINB)
 render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total_camera,
                   const mk_snapshot_view *__restrict__ snaps, RenderWorkspace *ws, RayRecord *q64, RayRecord *q32,
-                  long long capacity, const mk_job *job, int mode, const double *__restrict__ cam) {
+                  long long capacity, const mk_job *job, int mode, const float4 *__restrict__ cam) {
     if (job) {
         nreq = job->nreq;
         total_camera = job->total_rays;
@@ -1250,17 +1260,11 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
         const long long idx = fetch(!active && !exhausted, counter, total);
         if (idx == -1) exhausted = true;
         if (idx >= 0 && (SRC != SRC_CAMERA || ray_in_request(reqs, nreq, idx))) {
-            double s64[8];
+            double s64[8];  // a queue record's state
             if (SRC == SRC_CAMERA) {
                 ray = idx;
                 rq = find_request(reqs, nreq, ray);
                 pix = ray - reqs[rq].ray_offset;
-                if (cam) {  // precomputed by camera_states_kernel
-                #pragma unroll
-                    for (int i = 0; i < 8; i++) s64[i] = cam[8 * ray + i];
-                } else {
-                    camera_ray(reqs[rq].camera, pix, s64);
-                }
                 steps = nsamples = 0;
                 max_tau = 0.0f;
 #pragma unroll
@@ -1289,8 +1293,27 @@ render_f32_kernel(const mk_request *__restrict__ reqs, int nreq, long long total
                 finish_ray_f32(R, pix, I, Ic, steps, MK_RAY_NAN, nsamples, max_tau, ws);
             } else {
                 const ReqF32 &Q = s_req[rq];
+                if (SRC == SRC_CAMERA) {
+                    if (cam) {  // precomputed by camera_states_kernel
+                        const float4 c0 = cam[4 * ray], c1 = cam[4 * ray + 1], c2 = cam[4 * ray + 2],
+                                     c3 = cam[4 * ray + 3];
+                        X[0] = {c0.x, c0.y};
+                        X[1] = {c0.z, c0.w};
+                        X[2] = {c1.x, c1.y};
+                        X[3] = {c1.z, c1.w};
+                        K[0] = {c2.x, c2.y};
+                        K[1] = {c2.z, c2.w};
+                        K[2] = {c3.x, c3.y};
+                        K[3] = {c3.z, c3.w};
+                    } else if (Q.cam_grid) {
+                        camera_ray_pair(Q.cam, Q.cam_pixels, pix, X, K);
+                    } else {
+                        camera_pair(R.camera, pix, X, K);
+                    }
+                } else {
 #pragma unroll
-                for (int i = 0; i < 4; i++) { X[i] = f2_from(s64[i]); K[i] = f2_from(s64[4 + i]); }
+                    for (int i = 0; i < 4; i++) { X[i] = f2_from(s64[i]); K[i] = f2_from(s64[4 + i]); }
+                }
                 KerrPoint<float> m;
                 kerr_accel(X[1].hi, X[2].hi, X[3].hi, K[0].hi, K[1].hi, K[2].hi, K[3].hi, Q.a, d1[0], d1[1], d1[2],
                            d1[3], m);
@@ -1496,10 +1519,10 @@ static int launch_render(const mk_request *reqs_dev, int32_t nreq, int64_t total
     RayRecord *q64 = (RayRecord *)((char *)workspace_dev + WS_HEADER);
     RayRecord *q32 = q64 + max_rays;
     const long long cap = (long long)max_rays;
-    double *cam = nullptr;
+    float4 *cam = nullptr;
     if (camera_precompute(max_rays, precision) &&
-        workspace_bytes >= ws_base(max_rays, precision) + 8 * sizeof(double) * (size_t)max_rays) {
-        cam = (double *)(q32 + max_rays);
+        workspace_bytes >= ws_base(max_rays, precision) + 4 * sizeof(float4) * (size_t)max_rays) {
+        cam = reinterpret_cast<float4 *>(q32 + max_rays);
         const int64_t grid = std::min<int64_t>((max_rays + RENDER_THREADS - 1) / RENDER_THREADS,
                                                (int64_t)device_sm_count() * 16);
         camera_states_kernel<<<(unsigned)grid, RENDER_THREADS, 0, st>>>(reqs_dev, nreq, (long long)total_rays,
