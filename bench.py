@@ -66,7 +66,7 @@ CHAIN_FLOOR_CYCLES = 1270
 # near-hole pipeline) from `ncu --set full -k regex:render_zone_kernel -s 3
 # -c 1`, both over
 # `python bench.py --precision mixed --steps 2 --warmup 3 --quick --serving 0 --sampling-rays 0`
-NCU_TRAFFIC_RENDER256 = {"A": 106.92e6 + 3.01e6, "B": 76.75e6 + 1.63e6, "C": 113.40e6 + 0.16e6}
+NCU_TRAFFIC_RENDER256 = {"A": 106.92e6 + 3.01e6, "B": 76.74e6 + 1.58e6, "C": 113.40e6 + 0.16e6}
 
 # FP64 FLOP (DFMA = 2) per point of the standalone sampling stage, from ncu's
 # DADD/DMUL/DFMA thread-instruction counters on fluid_scalars_kernel (64x64
