@@ -64,7 +64,7 @@ int main() {
     double worst_x = 0, worst_k = 0;
     int rays = 0, nan_ok = 1;
     const double spins[] = {0.0, 0.5, 0.94, 0.999};
-    const double incs[] = {1.0, 17.0, 60.0, 85.0, 90.0};
+    const double incs[] = {0.0, 1.0, 17.0, 60.0, 85.0, 90.0, 180.0};
     const double fovs[] = {0.05, 20.0, 50.0};
     const double dists[] = {100.0, 1000.0, 1e4};
     const int sizes[] = {7, 64};
