@@ -48,10 +48,10 @@ def test_double_float_null_renormalisation(tmp_path):
 def test_double_float_camera_rays(tmp_path):
     """camera_ray_pair (mk_kerr.cuh), the mixed forms' camera rays in
     double-float, against the reference's construction in long double over
-    4 spins x 7 inclinations (0-180 deg) x 3 fields of view x 3 distances x 2 grid
-    sizes: positions within 1e-13 and wavevectors within 1e-11 of their
-    norms, and NaN exactly where the reference has no direction (the centre
-    of an odd grid)."""
+    4 spins x 7 inclinations (0-180 deg) x 3 fields of view x 3 distances x
+    2 grid sizes: positions within 1e-13 and wavevectors within 1e-11 of
+    their norms, and NaN exactly where the reference has no direction (the
+    centre of an odd grid)."""
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
