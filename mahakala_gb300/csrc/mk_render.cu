@@ -22,15 +22,15 @@
 //   MK_FP64  one launch, every operation in FP64 (the reference's x64).
 //   MK_MIXED three launches, A on the caller's stream, then B on it and C
 //   on a side stream forked after A and joined back after C:
-//     A  FP32 from the camera.  A ray whose radius drops below R_FP64 (3 M),
-//        or that moves inward inside R_TURN (6 M, where photon-ring rays
-//        reach their turning points), is handed to the near-hole queue; a
-//        ray moving outward past R_TURN is parked in the FP32 queue (records
-//        in binary64);
+//     A  FP32 from the camera (camera rays in double-float).  A ray whose
+//        radius drops below R_FP64 (3 M), or that moves inward inside
+//        R_TURN (6 M, where photon-ring rays reach their turning points), is
+//        handed to the near-hole queue; a ray moving outward past R_TURN is
+//        parked in the FP32 queue (records in binary64);
 //     B  the near-hole queue (render_zone_kernel): the float-pair state is
-//        renormalised to null in binary64 on entry and at each radial
-//        turning point inside R_TURN; the kernel carries the ray on to its
-//        end;
+//        renormalised to null on entry (binary64) and at each radial
+//        turning point inside R_TURN (double-float); the kernel carries the
+//        ray on to its end;
 //     C  the FP32 queue (render_f32_kernel over the queue), beside B: the
 //        two share no ray and no counter.
 //   MK_MIXED_STRICT: phase B integrates the near-hole geodesic entirely in
@@ -39,7 +39,8 @@
 //   Splitting by precision keeps each warp uniform: on a part whose FP64
 //   rate is 1/64 of FP32, one FP64 lane would stall the other 31.  The
 //   intensity accumulates with a compensated (Kahan) FP32 sum and the
-//   transmission product in FP32; both move to FP64 with the ray.
+//   transmission product in FP32, in MK_MIXED's phase B too; the strict
+//   and DF forms move both to FP64 with the ray.
 #include <string.h>
 
 #include <algorithm>
@@ -857,10 +858,10 @@ __device__ __forceinline__ void zone_integrate(const mk_request *__restrict__ re
     bool active = false, exhausted = false;
     int steps = 0, nmax = 0, zone_steps = 0, run = 0, run_max = 0, b_steps = 0, ray = -1;
     // float-pair state (X, K) throughout, as in the FP32 phases; near the
-    // hole the wavevector is renormalised to null in binary64 on entry and
-    // at every radial turning point.  After the ray leaves outward the
-    // integration continues here to the ray's end (its remaining ~250 steps
-    // would otherwise wait for a third launch).
+    // hole the wavevector is renormalised to null on entry (binary64) and
+    // at every radial turning point (double-float).  After the ray leaves
+    // outward the integration continues here to the ray's end (its
+    // remaining ~250 steps would otherwise wait for a third launch).
     bool inzone = true;
     double bhspin = 0.0;
     dd ad(0.0f);  // the spin as a float pair
