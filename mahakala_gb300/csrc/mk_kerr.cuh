@@ -422,8 +422,8 @@ __host__ __device__ __forceinline__ double grid_coord_of(int i, double step, dou
 
 // Initial state of grid-camera pixel p as float pairs, in double-float
 // arithmetic (~1e-13 relative; the binary64 camera_ray below puts ~300
-// instructions per ray on the FP64 pipe, which every warp of the mixed
-// forms' camera phase waited on at its start).  The image-plane
+// instructions per ray on the FP64 pipe, 1/64 of the FP32 rate on this
+// part; here only the two grid coordinates are binary64).  The image-plane
 // coordinates (x, y) are the binary64 grid's (so the image centre of an odd
 // grid is exactly 0 when binary64 rounds it there); the ray starts at that
 // point moved to the camera (geodesics.py:121-132, 168-179): position
