@@ -1,5 +1,6 @@
 """The C-ABI library loads without a GPU and exports every symbol the public
-header declares, with the struct layouts the Python binding assumes."""
+header declares, with the struct layouts the Python binding assumes; a C
+program includes the header and links the library."""
 
 import ctypes
 import os
@@ -112,3 +113,21 @@ def test_mixed_request_limit_without_gpu(lib):
         _lib.call("mk_render", c.addressof(ws), n, 10, c.addressof(ws), 1, _lib.MK_MIXED, c.addressof(ws),
                   lib.mk_render_workspace_bytes(10, _lib.MK_MIXED), None)
     assert e.value.code == _lib.MK_ERR_LIMIT
+
+
+def test_c_host_compiles_links_and_calls(lib, tmp_path):
+    """The header as C11 (-pedantic -Werror) in a C program linked against
+    the library: struct layouts as a C compiler lays them out equal the
+    library's, and the GPU-free entry points answer (tests/abi_c_check.c)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    build_dir = os.path.join(ROOT, "mahakala_gb300", "_build")
+    exe = tmp_path / "abi_c_check"
+    subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "abi_c_check.c"), "-L", build_dir, "-lmahakala_gb300",
+                    f"-Wl,-rpath,{build_dir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout + out.stderr
